@@ -1,0 +1,1032 @@
+// ParticleFilter on the device: init, predict, update (blend, normalise, mean),
+// resample (ParticleFilter.cpp:46-222).
+//
+// Device layout: particles as structure-of-arrays, pose float4 (x, y, z, yaw) plus
+// w, wp, wr float arrays, double-buffered so resample gathers into the spare copy.
+// All normalisation sums, the mean and the resampling prefix are exact (integer
+// X320 sums, see exact.cuh): they do not depend on summation order, launch shape
+// or batching, and each is rounded once (to double) where a value is needed.
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
+#include "bulk.cuh"
+#include "exact.cuh"
+#include "grid.cuh"
+#include "philox.cuh"
+
+using namespace amcl;
+
+namespace
+{
+enum Acc
+{
+  ACC_WP = 0,
+  ACC_WR,
+  ACC_W,
+  ACC_W2,  // sum of the normalised weights
+  ACC_M1,  // 4 accumulators: sum w*x, w*y, w*z, w*a
+  ACC_M2 = ACC_M1 + 4,  // 4 accumulators: sum w*x^2, ...
+  ACC_COUNT = ACC_M2 + 4
+};
+constexpr int NDIG = 10;
+constexpr int NT = 256;  // threads per block of the per-particle kernels
+
+struct PFStats
+{
+  double sum_wp, sum_wr, sum_w, sum_w2;
+  double mean[4];
+  double var[4];
+  float mean_f[4];
+  int err;
+  int pad;
+};
+
+__device__ __forceinline__ double acc_value(const unsigned long long* acc, int k)
+{
+  return x320_to_double(x320_from_digits(acc + k * NDIG));
+}
+
+// Exact two-product of floats via FMA: a*b = p + e exactly (e rounded only if it
+// underflows; the oracle rounds the same residual the same way).
+__device__ __forceinline__ void two_prod(float a, float b, float& p, float& e)
+{
+  p = __fmul_rn(a, b);
+  e = __fmaf_rn(a, b, -p);
+}
+
+// Block-wide exact sum of one value per thread added to digits `dst`.
+__device__ __forceinline__ void block_exact_add(X320 v, unsigned long long* dst, X320* s_part)
+{
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  v = x320_warp_sum(v);
+  __syncthreads();
+  if (lane == 0)
+    s_part[wid] = v;
+  __syncthreads();
+  if (wid == 0)
+  {
+    X320 t = lane < nw ? s_part[lane] : x320_zero();
+    t = x320_warp_sum(t);
+    if (lane == 0)
+      x320_atomic_add(dst, t);
+  }
+}
+
+// ---- update: blend (ParticleFilter.cpp:157-180) ------------------------------------------
+__global__ __launch_bounds__(NT) void k_blend(uint32_t n, const uint8_t* __restrict__ inmap, float* __restrict__ wp,
+                                             float* __restrict__ wr, float* __restrict__ w, double alpha,
+                                             unsigned long long* acc)
+{
+  __shared__ double s_sum[2];
+  __shared__ X320 s_part[NT / 32];
+  if (threadIdx.x == 0)
+  {
+    s_sum[0] = acc_value(acc, ACC_WP);
+    s_sum[1] = acc_value(acc, ACC_WR);
+  }
+  __syncthreads();
+  const double sp = s_sum[0], sr = s_sum[1];
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  float wv = 0.0f;
+  if (i < n)
+  {
+    // wp /= wtp for every particle, stale values of out-of-map particles included.
+    const float a = sp > 0 ? __double2float_rn(__ddiv_rn(static_cast<double>(wp[i]), sp)) : 0.0f;
+    const float b = sr > 0 ? __double2float_rn(__ddiv_rn(static_cast<double>(wr[i]), sr)) : 0.0f;
+    wp[i] = a;
+    wr[i] = b;
+    if (inmap[i])
+      wv = __double2float_rn(
+          __dadd_rn(__dmul_rn(static_cast<double>(a), alpha), __dmul_rn(static_cast<double>(b), __dsub_rn(1.0, alpha))));
+    w[i] = wv;
+  }
+  block_exact_add(x320_from_float(wv), acc + ACC_W * NDIG, s_part);
+}
+
+// ---- normalise w, accumulate the mean terms and the per-block resample sums ---------------
+// (ParticleFilter.cpp:182-195 for update, :79-92 for init)
+__global__ __launch_bounds__(NT) void k_normalize(uint32_t n, const float4* __restrict__ pose, float* __restrict__ w,
+                                                 unsigned long long* acc, X320* __restrict__ blocksum)
+{
+  __shared__ double s_tot;
+  __shared__ X320 s_part[NT / 32];
+  if (threadIdx.x == 0)
+    s_tot = acc_value(acc, ACC_W);
+  __syncthreads();
+  const double tot = s_tot;
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  float wv = 0.0f;
+  float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (i < n)
+  {
+    wv = tot > 0 ? __double2float_rn(__ddiv_rn(static_cast<double>(w[i]), tot)) : 0.0f;
+    w[i] = wv;
+    p = pose[i];
+  }
+  const X320 xw = x320_from_float(wv);
+  // sum of normalised weights: also the resample block sum
+  {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    X320 v = x320_warp_sum(xw);
+    if (lane == 0)
+      s_part[wid] = v;
+    __syncthreads();
+    if (wid == 0)
+    {
+      X320 t = lane < static_cast<int>(NT / 32) ? s_part[lane] : x320_zero();
+      t = x320_warp_sum(t);
+      if (lane == 0)
+      {
+        blocksum[blockIdx.x] = t;
+        x320_atomic_add(acc + ACC_W2 * NDIG, t);
+      }
+    }
+  }
+  const float c[4] = { p.x, p.y, p.z, p.w };
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+  {
+    float hi, lo;
+    two_prod(wv, c[k], hi, lo);
+    block_exact_add(x320_add(x320_from_float(hi), x320_from_float(lo)), acc + (ACC_M1 + k) * NDIG, s_part);
+    // w*c^2 = w*(s + t) with c*c = s + t exactly; each product split again.
+    float s, t, h1, l1, h2, l2;
+    two_prod(c[k], c[k], s, t);
+    two_prod(wv, s, h1, l1);
+    two_prod(wv, t, h2, l2);
+    X320 q = x320_add(x320_add(x320_from_float(h1), x320_from_float(l1)),
+                      x320_add(x320_from_float(h2), x320_from_float(l2)));
+    block_exact_add(q, acc + (ACC_M2 + k) * NDIG, s_part);
+  }
+}
+
+__global__ void k_finalize_stats(const unsigned long long* acc, PFStats* st)
+{
+  if (threadIdx.x != 0 || blockIdx.x != 0)
+    return;
+  st->sum_wp = acc_value(acc, ACC_WP);
+  st->sum_wr = acc_value(acc, ACC_WR);
+  st->sum_w = acc_value(acc, ACC_W);
+  const double s2 = acc_value(acc, ACC_W2);
+  st->sum_w2 = s2;
+  for (int k = 0; k < 4; ++k)
+  {
+    const double m1 = acc_value(acc, ACC_M1 + k);
+    const double m2 = acc_value(acc, ACC_M2 + k);
+    st->mean[k] = m1;  // the reference's mean is sum w*x of the normalised weights
+    st->mean_f[k] = __double2float_rn(m1);
+    if (s2 > 0)
+    {
+      const double mu = __ddiv_rn(m1, s2);
+      st->var[k] = __dsub_rn(__ddiv_rn(m2, s2), __dmul_rn(mu, mu));
+    }
+    else
+      st->var[k] = 0.0;
+  }
+}
+
+// ---- predict (ParticleFilter.cpp:97-119) ------------------------------------------------------
+struct PredictArgs
+{
+  uint32_t n;
+  uint32_t seed_lo, seed_hi;
+  uint64_t step;
+  float sx, sy, sz, sa;  // (float) |delta * mod|, the normal_distribution<float> stddev
+  double dx, dy, dz, da;
+  float* draws;  // optional 4 per particle
+};
+
+__global__ __launch_bounds__(NT) void k_predict(float4* __restrict__ pose, PredictArgs a)
+{
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n)
+    return;
+  Philox4 c;
+  c.v[0] = i;
+  c.v[1] = static_cast<uint32_t>(a.step);
+  c.v[2] = static_cast<uint32_t>(a.step >> 32);
+  c.v[3] = RNG_TAG_PREDICT;
+  float z[4];
+  normals4(philox4x32_10(c, a.seed_lo, a.seed_hi), z);
+  if (a.draws)
+    reinterpret_cast<float4*>(a.draws)[i] = make_float4(z[0], z[1], z[2], z[3]);
+  float4 p = pose[i];
+  // ranGaussian(0, dev) = z * (float)dev + 0.0f  (normal_distribution<float>)
+  const float gx = fadd(fmul(z[0], a.sx), 0.0f);
+  const float gy = fadd(fmul(z[1], a.sy), 0.0f);
+  const float gz = fadd(fmul(z[2], a.sz), 0.0f);
+  const float ga = fadd(fmul(z[3], a.sa), 0.0f);
+  double sd, cd;
+  sincos(static_cast<double>(p.w), &sd, &cd);
+  const float sa = __double2float_rn(sd), ca = __double2float_rn(cd);
+  const float rx = __double2float_rn(__dadd_rn(a.dx, static_cast<double>(gx)));
+  const float ry = __double2float_rn(__dadd_rn(a.dy, static_cast<double>(gy)));
+  p.x = fadd(p.x, fsub(fmul(ca, rx), fmul(sa, ry)));
+  p.y = fadd(p.y, fadd(fmul(sa, rx), fmul(ca, ry)));
+  p.z = __double2float_rn(__dadd_rn(static_cast<double>(p.z), __dadd_rn(a.dz, static_cast<double>(gz))));
+  p.w = __double2float_rn(__dadd_rn(static_cast<double>(p.w), __dadd_rn(a.da, static_cast<double>(ga))));
+  pose[i] = p;
+}
+
+// ---- init (ParticleFilter.cpp:46-77) ----------------------------------------------------------
+struct InitArgs
+{
+  uint32_t n;
+  uint32_t seed_lo, seed_hi;
+  uint64_t step;
+  float x, y, z, a;
+  float xd, yd, zd, ad;
+  float gc1, gc2;
+  float* draws;
+};
+
+__global__ __launch_bounds__(NT) void k_init(float4* __restrict__ pose, float* __restrict__ w, float* __restrict__ wp,
+                                            float* __restrict__ wr, InitArgs a, unsigned long long* acc)
+{
+  __shared__ X320 s_part[NT / 32];
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  float wv = 0.0f;
+  if (i < a.n)
+  {
+    float4 p = make_float4(a.x, a.y, a.z, a.a);
+    wv = a.gc1;
+    if (i > 0)
+    {
+      Philox4 c;
+      c.v[0] = i;
+      c.v[1] = static_cast<uint32_t>(a.step);
+      c.v[2] = static_cast<uint32_t>(a.step >> 32);
+      c.v[3] = RNG_TAG_INIT;
+      float zz[4];
+      normals4(philox4x32_10(c, a.seed_lo, a.seed_hi), zz);
+      if (a.draws)
+        reinterpret_cast<float4*>(a.draws)[i] = make_float4(zz[0], zz[1], zz[2], zz[3]);
+      p.x = fadd(a.x, fadd(fmul(zz[0], a.xd), 0.0f));
+      p.y = fadd(a.y, fadd(fmul(zz[1], a.yd), 0.0f));
+      p.z = fadd(a.z, fadd(fmul(zz[2], a.zd), 0.0f));
+      p.w = fadd(a.a, fadd(fmul(zz[3], a.ad), 0.0f));
+      const float dx = fsub(p.x, a.x), dy = fsub(p.y, a.y), dz = fsub(p.z, a.z);
+      const float dist = __fsqrt_rn(fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz)));
+      const float e = __double2float_rn(exp(static_cast<double>(fmul(fmul(-dist, dist), a.gc2))));
+      wv = fmul(a.gc1, e);
+    }
+    else if (a.draws)
+      reinterpret_cast<float4*>(a.draws)[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+    pose[i] = p;
+    w[i] = wv;
+    wp[i] = 0.0f;  // Particle() zero-initialises wp, wr (ParticleFilter.h:46)
+    wr[i] = 0.0f;
+  }
+  block_exact_add(x320_from_float(wv), acc + ACC_W * NDIG, s_part);
+}
+
+// ---- resample (ParticleFilter.cpp:198-222) ---------------------------------------------------
+// u_m = r + factor*m in float; index[m] = first i with C_i >= u_m where C is the
+// inclusive prefix of w; for each particle hi_i = #{m : u_m <= C_i} (u is
+// non-decreasing in m), so index[m] = first i with hi_i > m.
+
+__device__ __forceinline__ float u_of(float r, float factor, uint32_t m) { return fadd(r, fmul(factor, static_cast<float>(m))); }
+
+__global__ __launch_bounds__(NT) void k_block_sums(uint32_t n, const float* __restrict__ w, X320* __restrict__ blocksum)
+{
+  __shared__ X320 s_part[NT / 32];
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  X320 v = x320_from_float(i < n ? w[i] : 0.0f);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  v = x320_warp_sum(v);
+  if (lane == 0)
+    s_part[wid] = v;
+  __syncthreads();
+  if (wid == 0)
+  {
+    X320 t = lane < static_cast<int>(NT / 32) ? s_part[lane] : x320_zero();
+    t = x320_warp_sum(t);
+    if (lane == 0)
+      blocksum[blockIdx.x] = t;
+  }
+}
+
+// Exact inclusive prefix C_i, then hi_i by binary search over m.
+__global__ __launch_bounds__(NT) void k_prefix_hi(uint32_t n, const float* __restrict__ w,
+                                                 const X320* __restrict__ blocksum, float r, float factor,
+                                                 int32_t* __restrict__ hi)
+{
+  __shared__ X320 s_scan[NT / 32];
+  __shared__ X320 s_base;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  // exclusive prefix of the block sums before this block
+  if (wid == 0)
+  {
+    X320 t = x320_zero();
+    for (uint32_t b = lane; b < blockIdx.x; b += 32)
+      t = x320_add(t, blocksum[b]);
+    t = x320_warp_sum(t);
+    if (lane == 0)
+      s_base = t;
+  }
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const X320 own = x320_from_float(i < n ? w[i] : 0.0f);
+  // warp inclusive scan
+  X320 x = own;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1)
+  {
+    X320 y;
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+      y.w[k] = __shfl_up_sync(0xFFFFFFFFu, x.w[k], o);
+    if (lane >= o)
+      x = x320_add(x, y);
+  }
+  if (lane == 31)
+    s_scan[wid] = x;
+  __syncthreads();
+  X320 c = s_base;
+  for (int k = 0; k < wid; ++k)
+    c = x320_add(c, s_scan[k]);
+  c = x320_add(c, x);  // inclusive prefix C_i
+  if (i >= n)
+    return;
+  uint32_t lo = 0, up = n;
+  while (lo < up)
+  {
+    const uint32_t mid = (lo + up) >> 1;
+    if (x320_cmp(x320_from_float(u_of(r, factor, mid)), c) <= 0)
+      lo = mid + 1;
+    else
+      up = mid;
+  }
+  hi[i] = static_cast<int32_t>(lo);
+}
+
+// The reference's float running sum c += w (ParticleFilter.cpp:203,214), one thread.
+__global__ void k_prefix_f32(uint32_t n, const float* __restrict__ w, float* __restrict__ cum)
+{
+  if (threadIdx.x != 0 || blockIdx.x != 0)
+    return;
+  float c = 0.0f;
+  for (uint32_t i = 0; i < n; ++i)
+  {
+    c = i == 0 ? w[0] : fadd(c, w[i]);
+    cum[i] = c;
+  }
+}
+
+__global__ __launch_bounds__(NT) void k_hi_from_f32(uint32_t n, const float* __restrict__ cum, float r, float factor,
+                                                   int32_t* __restrict__ hi)
+{
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n)
+    return;
+  const float c = cum[i];
+  uint32_t lo = 0, up = n;
+  while (lo < up)
+  {
+    const uint32_t mid = (lo + up) >> 1;
+    if (!(u_of(r, factor, mid) > c))  // the reference advances while u > c
+      lo = mid + 1;
+    else
+      up = mid;
+  }
+  hi[i] = static_cast<int32_t>(lo);
+}
+
+__global__ __launch_bounds__(NT) void k_gather(uint32_t n, const int32_t* __restrict__ hi, const float4* __restrict__ pose,
+                                              const float* __restrict__ wp, const float* __restrict__ wr,
+                                              float4* __restrict__ pose_o, float* __restrict__ w_o,
+                                              float* __restrict__ wp_o, float* __restrict__ wr_o, float factor,
+                                              int32_t* __restrict__ idx_o)
+{
+  const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= n)
+    return;
+  uint32_t lo = 0, up = n;
+  while (lo < up)
+  {
+    const uint32_t mid = (lo + up) >> 1;
+    if (static_cast<uint32_t>(hi[mid]) > m)
+      up = mid;
+    else
+      lo = mid + 1;
+  }
+  // lo == n: the reference runs past its array (reads p_[N]); clamp to the last particle.
+  const uint32_t src = lo < n ? lo : n - 1;
+  pose_o[m] = pose[src];
+  wp_o[m] = wp[src];
+  wr_o[m] = wr[src];
+  w_o[m] = factor;  // new_p[m].w = factor (ParticleFilter.cpp:217)
+  if (idx_o)
+    idx_o[m] = static_cast<int32_t>(src);
+}
+}  // namespace
+
+// ---- host handle ----------------------------------------------------------------------------------
+
+struct amcl_pf_s
+{
+  StreamHolder st;
+  uint32_t n = 0;
+  uint32_t cap = 0;
+  bool initialized = false;
+  uint64_t seed = 0;
+  uint64_t step = 0;
+  int cur = 0;
+  DevBuf pose[2], w[2], wp[2], wr[2];
+  DevBuf inmap, acc, stats, blocksum, hi, ridx, cum, scratch, cloud, ranges, draws, err;
+  PinnedBuf h_cloud, h_ranges, h_stats;
+  cudaEvent_t staged = nullptr;
+  bool staged_pending = false;
+  bool blocksum_valid = false;
+  bool record = false;
+  bool have_ridx = false;
+  int opt_cloud_sum = 0, opt_prefix = 0, opt_kernel = 0;
+  Profiler prof;
+  std::mutex mu;
+};
+
+namespace
+{
+int pf_reserve(amcl_pf_s* pf, uint32_t n)
+{
+  if (n <= pf->cap && pf->pose[0].p)
+    return AMCL_OK;
+  int rc;
+  const size_t nb = ceil_div(n, NT);
+  for (int b = 0; b < 2; ++b)
+    if ((rc = pf->pose[b].ensure(n * 16ull)) || (rc = pf->w[b].ensure(n * 4ull)) || (rc = pf->wp[b].ensure(n * 4ull)) ||
+        (rc = pf->wr[b].ensure(n * 4ull)))
+      return rc;
+  if ((rc = pf->inmap.ensure(n)) || (rc = pf->blocksum.ensure(nb * sizeof(X320))) || (rc = pf->hi.ensure(n * 4ull)) ||
+      (rc = pf->ridx.ensure(n * 4ull)) || (rc = pf->draws.ensure(n * 16ull)))
+    return rc;
+  pf->cap = n;
+  return AMCL_OK;
+}
+
+int pf_common_alloc(amcl_pf_s* pf)
+{
+  int rc;
+  if ((rc = pf->acc.ensure(ACC_COUNT * NDIG * 8)) || (rc = pf->stats.ensure(sizeof(PFStats))) ||
+      (rc = pf->err.ensure(sizeof(int))) || (rc = pf->h_stats.ensure(sizeof(PFStats))))
+    return rc;
+  return AMCL_OK;
+}
+
+int pf_check_err(amcl_pf_s* pf)
+{
+  int e = 0;
+  AMCL_CUDA_TRY(cudaMemcpyAsync(&e, pf->err.p, sizeof(int), cudaMemcpyDeviceToHost, pf->st.s));
+  AMCL_CUDA_TRY(cudaStreamSynchronize(pf->st.s));
+  if (e)
+  {
+    cudaMemsetAsync(pf->err.p, 0, sizeof(int), pf->st.s);
+    return fail(AMCL_ETIMEDOUT, "a bounded device-side wait gave up (error code " + std::to_string(e) + ")");
+  }
+  return AMCL_OK;
+}
+
+// Normalise w (exact total), accumulate mean terms, write block sums, finalize stats.
+int pf_normalize_and_stats(amcl_pf_s* pf)
+{
+  const unsigned nb = ceil_div(pf->n, NT);
+  unsigned long long* acc = pf->acc.as<unsigned long long>();
+  k_normalize<<<nb, NT, 0, pf->st.s>>>(pf->n, pf->pose[pf->cur].as<float4>(), pf->w[pf->cur].as<float>(), acc,
+                                        pf->blocksum.as<X320>());
+  AMCL_LAUNCH_CHECK("k_normalize");
+  k_finalize_stats<<<1, 32, 0, pf->st.s>>>(acc, pf->stats.as<PFStats>());
+  AMCL_LAUNCH_CHECK("k_finalize_stats");
+  pf->blocksum_valid = true;
+  return AMCL_OK;
+}
+
+int pf_update_impl(amcl_pf_s* pf, amcl_grid_s* g, const float4* cloud_dev, uint32_t n_pts, const float* ranges4,
+                   uint32_t nr, double alpha, double sigma, double roll, double pitch, bool ranges_only)
+{
+  cudaStream_t s = pf->st.s;
+  int rc;
+  if (nr > 64)
+    return fail(AMCL_ERANGE, "update: more than 64 range measurements");
+  // Ranges to the device through pinned staging.
+  if (nr)
+  {
+    if ((rc = pf->h_ranges.ensure(nr * 16)) || (rc = pf->ranges.ensure(nr * 16)))
+      return rc;
+    std::memcpy(pf->h_ranges.p, ranges4, nr * 16);
+    AMCL_CUDA_TRY(cudaMemcpyAsync(pf->ranges.p, pf->h_ranges.p, nr * 16, cudaMemcpyHostToDevice, s));
+  }
+  AMCL_CUDA_TRY(cudaMemsetAsync(pf->acc.p, 0, ACC_COUNT * NDIG * 8, s));
+  WeightArgs a{};
+  a.pose = pf->pose[pf->cur].as<float4>();
+  a.P = pf->n;
+  a.cloud = cloud_dev;
+  a.N = n_pts;
+  // roll/pitch: float parameters of computeCloudWeight (Node passes doubles, narrowed
+  // at the call, ParticleFilter.cpp:145); sin/cos as float overloads.
+  const float rollf = static_cast<float>(roll), pitchf = static_cast<float>(pitch);
+  a.sr = sinf(rollf);  // computed once per update on the host, with the same libm
+  a.cr = cosf(rollf);
+  a.sp = sinf(pitchf);
+  a.cp = cosf(pitchf);
+  a.ranges = pf->ranges.as<float4>();
+  a.nr = nr;
+  a.k1 = static_cast<float>(1.f / (sigma * std::sqrt(2 * M_PI)));  // ParticleFilter.cpp:231
+  a.k2 = static_cast<float>(0.5f / (sigma * sigma));              // ParticleFilter.cpp:232
+  a.wp = pf->wp[pf->cur].as<float>();
+  a.wr = pf->wr[pf->cur].as<float>();
+  a.inmap = pf->inmap.as<uint8_t>();
+  unsigned long long* acc = pf->acc.as<unsigned long long>();
+  a.acc_wp = acc + ACC_WP * NDIG;
+  a.acc_wr = acc + ACC_WR * NDIG;
+  a.err = pf->err.as<int>();
+  a.cloud_sum = pf->opt_cloud_sum;
+  a.kernel = pf->opt_kernel ? pf->opt_kernel : choose_weight_kernel(pf->n, n_pts);
+  amcl_grid_s local;  // ranges-only: every particle counts as inside, no cloud
+  amcl_grid_s* gg = g;
+  if (ranges_only)
+  {
+    local.view = GridView{};
+    local.view.built = 1;
+    for (int k = 0; k < 3; ++k)
+    {
+      local.view.in_lo[k] = -INFINITY;
+      local.view.in_hi[k] = INFINITY;
+    }
+    local.view.storage = AMCL_GRID_F32;
+    a.N = 0;
+    a.kernel = 1;
+    gg = &local;
+  }
+  else
+    grid_apply_l2_window(g, s);
+  if (a.kernel == 2)
+  {
+    const uint64_t need = two_phase_scratch_floats(pf->n, a.N);
+    if ((rc = pf->scratch.ensure(need * 4)))
+      return rc;
+    a.scratch = pf->scratch.as<float>();
+    a.scratch_floats = pf->scratch.bytes / 4;
+  }
+  {
+    ProfScope ps(&pf->prof, s, AMCL_PROF_CLOUD_WEIGHT);
+    if ((rc = launch_cloud_weight(gg, a, s)))
+      return rc;
+  }
+  {
+    ProfScope ps(&pf->prof, s, AMCL_PROF_NORMALIZE);
+    const unsigned nb = ceil_div(pf->n, NT);
+    k_blend<<<nb, NT, 0, s>>>(pf->n, pf->inmap.as<uint8_t>(), pf->wp[pf->cur].as<float>(), pf->wr[pf->cur].as<float>(),
+                              pf->w[pf->cur].as<float>(), alpha, acc);
+    AMCL_LAUNCH_CHECK("k_blend");
+    if ((rc = pf_normalize_and_stats(pf)))
+      return rc;
+  }
+  return AMCL_OK;
+}
+
+int stage_host_cloud(amcl_pf_s* pf, const float* xyz, uint32_t n, uint32_t stride)
+{
+  int rc;
+  if ((rc = pf->h_cloud.ensure(std::max<size_t>(n, 1) * 16)) || (rc = pf->cloud.ensure(std::max<size_t>(n, 1) * 16)))
+    return rc;
+  if (pf->staged_pending)
+  {
+    cudaEventSynchronize(pf->staged);  // previous copy out of the pinned buffer done
+    pf->staged_pending = false;
+  }
+  pack_cloud(xyz, n, stride, pf->h_cloud.as<float4>());
+  if (n)
+    AMCL_CUDA_TRY(cudaMemcpyAsync(pf->cloud.p, pf->h_cloud.p, n * 16ull, cudaMemcpyHostToDevice, pf->st.s));
+  AMCL_CUDA_TRY(cudaEventRecord(pf->staged, pf->st.s));
+  pf->staged_pending = true;
+  return AMCL_OK;
+}
+
+int do_resample(amcl_pf_s* pf, float u01)
+{
+  cudaStream_t s = pf->st.s;
+  const uint32_t n = pf->n;
+  ProfScope ps(&pf->prof, s, AMCL_PROF_RESAMPLE);
+  // Host float arithmetic (IEEE single; the library is built with -ffp-contract=off).
+  const float factor = 1.f / static_cast<float>(n);  // ParticleFilter.cpp:201
+  const float r = factor * u01;                       // ParticleFilter.cpp:202
+  const unsigned nb = ceil_div(n, NT);
+  const int c = pf->cur, o = 1 - pf->cur;
+  if (pf->opt_prefix == 1)
+  {
+    int rc;
+    if ((rc = pf->cum.ensure(n * 4ull)))
+      return rc;
+    k_prefix_f32<<<1, 32, 0, s>>>(n, pf->w[c].as<float>(), pf->cum.as<float>());
+    AMCL_LAUNCH_CHECK("k_prefix_f32");
+    k_hi_from_f32<<<nb, NT, 0, s>>>(n, pf->cum.as<float>(), r, factor, pf->hi.as<int32_t>());
+    AMCL_LAUNCH_CHECK("k_hi_from_f32");
+  }
+  else
+  {
+    if (!pf->blocksum_valid)
+    {
+      k_block_sums<<<nb, NT, 0, s>>>(n, pf->w[c].as<float>(), pf->blocksum.as<X320>());
+      AMCL_LAUNCH_CHECK("k_block_sums");
+    }
+    k_prefix_hi<<<nb, NT, 0, s>>>(n, pf->w[c].as<float>(), pf->blocksum.as<X320>(), r, factor, pf->hi.as<int32_t>());
+    AMCL_LAUNCH_CHECK("k_prefix_hi");
+  }
+  k_gather<<<nb, NT, 0, s>>>(n, pf->hi.as<int32_t>(), pf->pose[c].as<float4>(), pf->wp[c].as<float>(),
+                             pf->wr[c].as<float>(), pf->pose[o].as<float4>(), pf->w[o].as<float>(),
+                             pf->wp[o].as<float>(), pf->wr[o].as<float>(), factor, pf->ridx.as<int32_t>());
+  AMCL_LAUNCH_CHECK("k_gather");
+  pf->cur = o;
+  pf->blocksum_valid = false;
+  pf->have_ridx = true;
+  return AMCL_OK;
+}
+
+float pf_next_uniform(amcl_pf_s* pf)
+{
+  Philox4 c;
+  c.v[0] = 0;
+  c.v[1] = static_cast<uint32_t>(pf->step);
+  c.v[2] = static_cast<uint32_t>(pf->step >> 32);
+  c.v[3] = RNG_TAG_RESAMPLE;
+  const Philox4 r = philox4x32_10(c, static_cast<uint32_t>(pf->seed), static_cast<uint32_t>(pf->seed >> 32));
+  pf->step += 1;
+  return u01_closed0(r.v[0]);
+}
+}  // namespace
+
+// ---- C ABI ----------------------------------------------------------------------------------------
+
+#define PF_GUARD(pf)                                  \
+  if (!(pf))                                          \
+    return fail(AMCL_EINVAL, "null filter handle");   \
+  std::lock_guard<std::mutex> lock_((pf)->mu)
+
+extern "C" int amcl_pf_create(amcl_pf_t* out, uint64_t seed, void* stream)
+{
+  if (!out)
+    return fail(AMCL_EINVAL, "amcl_pf_create: null out");
+  amcl_pf_s* pf = new amcl_pf_s();
+  int rc = pf->st.init(stream);
+  if (!rc)
+    rc = pf_common_alloc(pf);
+  if (!rc && cudaEventCreateWithFlags(&pf->staged, cudaEventDisableTiming) != cudaSuccess)
+    rc = fail(AMCL_ECUDA, "amcl_pf_create: cudaEventCreate failed");
+  if (!rc && (cudaMemsetAsync(pf->err.p, 0, sizeof(int), pf->st.s) != cudaSuccess ||
+              cudaMemsetAsync(pf->stats.p, 0, sizeof(PFStats), pf->st.s) != cudaSuccess))
+    rc = fail(AMCL_ECUDA, "amcl_pf_create: cudaMemset failed");
+  if (rc)
+  {
+    delete pf;
+    return rc;
+  }
+  pf->seed = seed;
+  *out = pf;
+  return AMCL_OK;
+}
+
+extern "C" int amcl_pf_destroy(amcl_pf_t pf)
+{
+  if (!pf)
+    return AMCL_OK;
+  cudaStreamSynchronize(pf->st.s);
+  if (pf->staged)
+    cudaEventDestroy(pf->staged);
+  delete pf;
+  return AMCL_OK;
+}
+
+extern "C" int amcl_pf_init(amcl_pf_t pf, int num_particles, float x, float y, float z, float a, float x_dev,
+                            float y_dev, float z_dev, float a_dev)
+{
+  PF_GUARD(pf);
+  const long long np = num_particles < 0 ? -static_cast<long long>(num_particles) : num_particles;  // abs()
+  if (np == 0)
+    return fail(AMCL_EINVAL, "amcl_pf_init: zero particles (the reference indexes p_[0])");
+  if (np > (1ll << 30))
+    return fail(AMCL_ERANGE, "amcl_pf_init: more than 2^30 particles");
+  int rc;
+  if ((rc = pf_reserve(pf, static_cast<uint32_t>(np))))
+    return rc;
+  pf->n = static_cast<uint32_t>(np);
+  pf->cur = 0;
+  cudaStream_t s = pf->st.s;
+  const float dev = std::max(std::max(x_dev, y_dev), z_dev);  // ParticleFilter.cpp:54
+  InitArgs ia{};
+  ia.n = pf->n;
+  ia.seed_lo = static_cast<uint32_t>(pf->seed);
+  ia.seed_hi = static_cast<uint32_t>(pf->seed >> 32);
+  ia.step = pf->step++;
+  ia.x = x;
+  ia.y = y;
+  ia.z = z;
+  ia.a = a;
+  ia.xd = static_cast<float>(static_cast<double>(x_dev));
+  ia.yd = static_cast<float>(static_cast<double>(y_dev));
+  ia.zd = static_cast<float>(static_cast<double>(z_dev));
+  ia.ad = static_cast<float>(static_cast<double>(a_dev));
+  ia.gc1 = static_cast<float>(1. / (dev * std::sqrt(2 * M_PI)));  // ParticleFilter.cpp:55
+  const float two_dev_dev = (2 * dev) * dev;
+  ia.gc2 = static_cast<float>(1. / two_dev_dev);                   // ParticleFilter.cpp:56
+  ia.draws = pf->record ? pf->draws.as<float>() : nullptr;
+  AMCL_CUDA_TRY(cudaMemsetAsync(pf->acc.p, 0, ACC_COUNT * NDIG * 8, s));
+  k_init<<<ceil_div(pf->n, NT), NT, 0, s>>>(pf->pose[0].as<float4>(), pf->w[0].as<float>(), pf->wp[0].as<float>(),
+                                           pf->wr[0].as<float>(), ia, pf->acc.as<unsigned long long>());
+  AMCL_LAUNCH_CHECK("k_init");
+  if ((rc = pf_normalize_and_stats(pf)))
+    return rc;
+  pf->initialized = true;
+  pf->have_ridx = false;
+  AMCL_CUDA_TRY(cudaStreamSynchronize(s));
+  return AMCL_OK;
+}
+
+extern "C" int amcl_pf_predict(amcl_pf_t pf, double odom_x_mod, double odom_y_mod, double odom_z_mod,
+                               double odom_a_mod, double delta_x, double delta_y, double delta_z, double delta_a)
+{
+  PF_GUARD(pf);
+  if (!pf->n)
+    return AMCL_OK;
+  PredictArgs pa{};
+  pa.n = pf->n;
+  pa.seed_lo = static_cast<uint32_t>(pf->seed);
+  pa.seed_hi = static_cast<uint32_t>(pf->seed >> 32);
+  pa.step = pf->step++;
+  pa.sx = static_cast<float>(std::fabs(delta_x * odom_x_mod));  // ParticleFilter.cpp:101-104
+  pa.sy = static_cast<float>(std::fabs(delta_y * odom_y_mod));
+  pa.sz = static_cast<float>(std::fabs(delta_z * odom_z_mod));
+  pa.sa = static_cast<float>(std::fabs(delta_a * odom_a_mod));
+  pa.dx = delta_x;
+  pa.dy = delta_y;
+  pa.dz = delta_z;
+  pa.da = delta_a;
+  pa.draws = pf->record ? pf->draws.as<float>() : nullptr;
+  ProfScope ps(&pf->prof, pf->st.s, AMCL_PROF_PREDICT);
+  k_predict<<<ceil_div(pf->n, NT), NT, 0, pf->st.s>>>(pf->pose[pf->cur].as<float4>(), pa);
+  AMCL_LAUNCH_CHECK("k_predict");
+  return AMCL_OK;
+}
+
+extern "C" int amcl_pf_update(amcl_pf_t pf, amcl_grid_t g, const float* xyz, uint32_t n, uint32_t stride_floats,
+                              const float* ranges4, uint32_t nr, double alpha, double sigma, double roll, double pitch)
+{
+  PF_GUARD(pf);
+  if (!g || (n && !xyz) || (nr && !ranges4) || stride_floats < 3)
+    return fail(AMCL_EINVAL, "amcl_pf_update: bad arguments");
+  if (!pf->n)
+    return AMCL_OK;
+  int rc;
+  if ((rc = stage_host_cloud(pf, xyz, n, stride_floats)))
+    return rc;
+  return pf_update_impl(pf, g, pf->cloud.as<float4>(), n, ranges4, nr, alpha, sigma, roll, pitch, false);
+}
+
+extern "C" int amcl_pf_update_dev(amcl_pf_t pf, amcl_grid_t g, const void* cloud_f4_dev, uint32_t n,
+                                  const float* ranges4, uint32_t nr, double alpha, double sigma, double roll,
+                                  double pitch)
+{
+  PF_GUARD(pf);
+  if (!g || (n && !cloud_f4_dev) || (nr && !ranges4) || (reinterpret_cast<uintptr_t>(cloud_f4_dev) & 15))
+    return fail(AMCL_EINVAL, "amcl_pf_update_dev: bad arguments (cloud must be 16-byte aligned float4)");
+  if (!pf->n)
+    return AMCL_OK;
+  return pf_update_impl(pf, g, static_cast<const float4*>(cloud_f4_dev), n, ranges4, nr, alpha, sigma, roll, pitch,
+                        false);
+}
+
+extern "C" int amcl_pf_update_ranges(amcl_pf_t pf, const float* ranges4, uint32_t nr, double alpha, double sigma)
+{
+  PF_GUARD(pf);
+  if (nr && !ranges4)
+    return fail(AMCL_EINVAL, "amcl_pf_update_ranges: bad arguments");
+  if (!pf->n)
+    return AMCL_OK;
+  return pf_update_impl(pf, nullptr, nullptr, 0, ranges4, nr, alpha, sigma, 0.0, 0.0, true);
+}
+
+extern "C" int amcl_pf_resample(amcl_pf_t pf)
+{
+  PF_GUARD(pf);
+  if (!pf->n)
+    return AMCL_OK;
+  const float u = pf_next_uniform(pf);
+  return do_resample(pf, u);
+}
+
+extern "C" int amcl_pf_resample_with(amcl_pf_t pf, float u01)
+{
+  PF_GUARD(pf);
+  if (!(u01 >= 0.0f && u01 < 1.0f))
+    return fail(AMCL_EINVAL, "amcl_pf_resample_with: u01 must be in [0, 1)");
+  if (!pf->n)
+    return AMCL_OK;
+  return do_resample(pf, u01);
+}
+
+extern "C" int amcl_pf_get_mean(amcl_pf_t pf, float mean7[7], double mean_var[8])
+{
+  PF_GUARD(pf);
+  if (!mean7)
+    return fail(AMCL_EINVAL, "amcl_pf_get_mean: null output");
+  for (int k = 0; k < 7; ++k)
+    mean7[k] = 0.0f;
+  if (mean_var)
+    for (int k = 0; k < 8; ++k)
+      mean_var[k] = 0.0;
+  if (!pf->initialized)
+    return AMCL_OK;  // mean_ of a fresh filter is Particle() = zeros
+  AMCL_CUDA_TRY(cudaMemcpyAsync(pf->h_stats.p, pf->stats.p, sizeof(PFStats), cudaMemcpyDeviceToHost, pf->st.s));
+  int rc = pf_check_err(pf);  // synchronises
+  if (rc)
+    return rc;
+  const PFStats* st = pf->h_stats.as<PFStats>();
+  for (int k = 0; k < 4; ++k)
+    mean7[k] = st->mean_f[k];
+  if (mean_var)
+    for (int k = 0; k < 4; ++k)
+    {
+      mean_var[k] = st->mean[k];
+      mean_var[4 + k] = st->var[k];
+    }
+  return AMCL_OK;
+}
+
+extern "C" int amcl_pf_is_initialized(amcl_pf_t pf, int* initialized)
+{
+  PF_GUARD(pf);
+  if (!initialized)
+    return fail(AMCL_EINVAL, "amcl_pf_is_initialized: null output");
+  *initialized = pf->initialized ? 1 : 0;
+  return AMCL_OK;
+}
+
+extern "C" int amcl_pf_size(amcl_pf_t pf, uint32_t* n)
+{
+  PF_GUARD(pf);
+  if (!n)
+    return fail(AMCL_EINVAL, "amcl_pf_size: null output");
+  *n = pf->n;
+  return AMCL_OK;
+}
+
+extern "C" int amcl_pf_get_particles(amcl_pf_t pf, float* p7, uint32_t cap)
+{
+  PF_GUARD(pf);
+  if (!p7 && cap)
+    return fail(AMCL_EINVAL, "amcl_pf_get_particles: null output");
+  const uint32_t m = std::min(cap, pf->n);
+  if (!m)
+    return AMCL_OK;
+  std::vector<float4> pose(m);
+  std::vector<float> w(m), wp(m), wr(m);
+  cudaStream_t s = pf->st.s;
+  AMCL_CUDA_TRY(cudaMemcpyAsync(pose.data(), pf->pose[pf->cur].p, m * 16ull, cudaMemcpyDeviceToHost, s));
+  AMCL_CUDA_TRY(cudaMemcpyAsync(w.data(), pf->w[pf->cur].p, m * 4ull, cudaMemcpyDeviceToHost, s));
+  AMCL_CUDA_TRY(cudaMemcpyAsync(wp.data(), pf->wp[pf->cur].p, m * 4ull, cudaMemcpyDeviceToHost, s));
+  AMCL_CUDA_TRY(cudaMemcpyAsync(wr.data(), pf->wr[pf->cur].p, m * 4ull, cudaMemcpyDeviceToHost, s));
+  int rc = pf_check_err(pf);
+  if (rc)
+    return rc;
+  for (uint32_t i = 0; i < m; ++i)
+  {
+    float* q = p7 + 7ull * i;
+    q[0] = pose[i].x;
+    q[1] = pose[i].y;
+    q[2] = pose[i].z;
+    q[3] = pose[i].w;
+    q[4] = w[i];
+    q[5] = wp[i];
+    q[6] = wr[i];
+  }
+  return AMCL_OK;
+}
+
+extern "C" int amcl_pf_set_particles(amcl_pf_t pf, const float* p7, uint32_t n)
+{
+  PF_GUARD(pf);
+  if (!p7 || !n)
+    return fail(AMCL_EINVAL, "amcl_pf_set_particles: need at least one particle");
+  if (n > (1u << 30))
+    return fail(AMCL_ERANGE, "amcl_pf_set_particles: more than 2^30 particles");
+  int rc;
+  if ((rc = pf_reserve(pf, n)))
+    return rc;
+  AMCL_CUDA_TRY(cudaStreamSynchronize(pf->st.s));
+  std::vector<float4> pose(n);
+  std::vector<float> w(n), wp(n), wr(n);
+  for (uint32_t i = 0; i < n; ++i)
+  {
+    const float* q = p7 + 7ull * i;
+    pose[i] = make_float4(q[0], q[1], q[2], q[3]);
+    w[i] = q[4];
+    wp[i] = q[5];
+    wr[i] = q[6];
+  }
+  pf->n = n;
+  pf->cur = 0;
+  cudaStream_t s = pf->st.s;
+  AMCL_CUDA_TRY(cudaMemcpyAsync(pf->pose[0].p, pose.data(), n * 16ull, cudaMemcpyHostToDevice, s));
+  AMCL_CUDA_TRY(cudaMemcpyAsync(pf->w[0].p, w.data(), n * 4ull, cudaMemcpyHostToDevice, s));
+  AMCL_CUDA_TRY(cudaMemcpyAsync(pf->wp[0].p, wp.data(), n * 4ull, cudaMemcpyHostToDevice, s));
+  AMCL_CUDA_TRY(cudaMemcpyAsync(pf->wr[0].p, wr.data(), n * 4ull, cudaMemcpyHostToDevice, s));
+  AMCL_CUDA_TRY(cudaStreamSynchronize(s));
+  pf->initialized = true;
+  pf->blocksum_valid = false;
+  pf->have_ridx = false;
+  return AMCL_OK;
+}
+
+extern "C" int amcl_pf_set_option(amcl_pf_t pf, int option, int64_t value)
+{
+  PF_GUARD(pf);
+  switch (option)
+  {
+    case AMCL_OPT_CLOUD_SUM:
+      if (value < 0 || value > 1)
+        return fail(AMCL_EINVAL, "AMCL_OPT_CLOUD_SUM: 0 or 1");
+      pf->opt_cloud_sum = static_cast<int>(value);
+      return AMCL_OK;
+    case AMCL_OPT_RESAMPLE_PREFIX:
+      if (value < 0 || value > 1)
+        return fail(AMCL_EINVAL, "AMCL_OPT_RESAMPLE_PREFIX: 0 or 1");
+      pf->opt_prefix = static_cast<int>(value);
+      return AMCL_OK;
+    case AMCL_OPT_WEIGHT_KERNEL:
+      if (value < 0 || value > 2)
+        return fail(AMCL_EINVAL, "AMCL_OPT_WEIGHT_KERNEL: 0, 1 or 2");
+      pf->opt_kernel = static_cast<int>(value);
+      return AMCL_OK;
+    case AMCL_OPT_SEED:
+      pf->seed = static_cast<uint64_t>(value);
+      pf->step = 0;
+      return AMCL_OK;
+    default:
+      return fail(AMCL_ENOTSUP, "amcl_pf_set_option: unknown option");
+  }
+}
+
+extern "C" int amcl_pf_record_draws(amcl_pf_t pf, int enable)
+{
+  PF_GUARD(pf);
+  pf->record = enable != 0;
+  return AMCL_OK;
+}
+
+extern "C" int amcl_pf_get_draws(amcl_pf_t pf, float* out, uint32_t cap_floats)
+{
+  PF_GUARD(pf);
+  if (!out && cap_floats)
+    return fail(AMCL_EINVAL, "amcl_pf_get_draws: null output");
+  const uint64_t m = std::min<uint64_t>(cap_floats, 4ull * pf->n);
+  if (m)
+    AMCL_CUDA_TRY(cudaMemcpyAsync(out, pf->draws.p, m * 4, cudaMemcpyDeviceToHost, pf->st.s));
+  AMCL_CUDA_TRY(cudaStreamSynchronize(pf->st.s));
+  return AMCL_OK;
+}
+
+extern "C" int amcl_pf_get_resample_index(amcl_pf_t pf, int32_t* out, uint32_t cap)
+{
+  PF_GUARD(pf);
+  if (!pf->have_ridx)
+    return fail(AMCL_ESTATE, "amcl_pf_get_resample_index: no resample since the last init/set");
+  const uint32_t m = std::min(cap, pf->n);
+  if (m)
+    AMCL_CUDA_TRY(cudaMemcpyAsync(out, pf->ridx.p, m * 4ull, cudaMemcpyDeviceToHost, pf->st.s));
+  AMCL_CUDA_TRY(cudaStreamSynchronize(pf->st.s));
+  return AMCL_OK;
+}
+
+extern "C" int amcl_pf_stream(amcl_pf_t pf, void** stream)
+{
+  if (!pf || !stream)
+    return fail(AMCL_EINVAL, "amcl_pf_stream: bad arguments");
+  *stream = pf->st.s;
+  return AMCL_OK;
+}
+
+extern "C" int amcl_pf_profile(amcl_pf_t pf, int enable)
+{
+  PF_GUARD(pf);
+  pf->prof.on = enable != 0;
+  return AMCL_OK;
+}
+
+extern "C" int amcl_pf_profile_read(amcl_pf_t pf, double ms[AMCL_PROF_COUNT], uint64_t launches[AMCL_PROF_COUNT],
+                                    int reset)
+{
+  PF_GUARD(pf);
+  pf->prof.collect();
+  for (int k = 0; k < AMCL_PROF_COUNT; ++k)
+  {
+    if (ms)
+      ms[k] = pf->prof.ms[k];
+    if (launches)
+      launches[k] = pf->prof.n[k];
+    if (reset)
+    {
+      pf->prof.ms[k] = 0;
+      pf->prof.n[k] = 0;
+    }
+  }
+  return AMCL_OK;
+}

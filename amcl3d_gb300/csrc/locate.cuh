@@ -1,0 +1,193 @@
+// Per-point arithmetic of Grid3d::computeCloudWeight (amcl3d/src/Grid3d.cpp:133-199),
+// reproduced bit for bit in float arithmetic on the GPU.
+//
+// The reference computes, per scan point s and particle (t, yaw):
+//   f   = (s.x*r00 + s.y*r01) + (s.z + 0)*r02          float, no FMA  (Grid3d.cpp:174)
+//   X   = (float)((double)f + (double(t.x) - min.x))   one double add  (Grid3d.cpp:155,174)
+//   ok  = X >= 0 && X < (max.x - min.x)                double compare  (Grid3d.cpp:178)
+//   ix  = (uint32)floor((double)X / res)               double divide   (Grid3d.cpp:181)
+//   ok &= ix < size_x                                                  (Grid3d.cpp:185)
+// FP64 runs at a small fraction of the FP32 rate on GB300, so the hot loop avoids
+// it:
+//  * the divide/floor/compare chain is replaced by exact float comparisons against a
+//    per-axis table T[k] = the smallest float X with floor(fl64(X / res)) >= k and a
+//    bound V = the smallest float X that fails a bound check (both computed on the
+//    host with the reference's own double arithmetic), so the cell index is decided
+//    by float compares that give exactly the reference's answer;
+//  * the double add is evaluated as a float-float sum (the particle offset split
+//    into H + L, Knuth's two-sum), which lands within one float ulp of the exact
+//    X; when any threshold lies within a safe margin of that estimate the point takes
+//    the exact FP64 path (one double add and a rounding), so every point gets the
+//    reference's X and cell index.
+#pragma once
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+namespace amcl
+{
+// Device view of one grid, passed by value to the weighting kernels.
+struct GridView
+{
+  const float* prob_f32;
+  const __half* prob_f16;
+  const uint8_t* prob_u8;
+  float u8_scale;
+  int storage;  // AMCL_GRID_*
+  uint32_t size[3];
+  uint32_t step_y, step_z;
+  // isIntoMap as float compares: x >= lo[a] && x < hi[a]  (Grid3d.cpp:207)
+  float in_lo[3], in_hi[3];
+  // locate tables
+  const float* T;  // x: [0, sx], y: [sx+1, sx+sy+1], z: ... (size+1 entries per axis)
+  uint32_t toff[3];
+  float V[3];
+  float inv_res[3];
+  double min[3];
+  uint64_t cells;
+  int built;
+};
+
+// Per-particle constants of the transform.
+struct PartXf
+{
+  float r[9];
+  float H[3], L[3];
+  double off[3];
+};
+
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+
+// Rotation of Grid3d.cpp:139-149 with the float overloads of sin/cos (what a ROS
+// build gets through <math.h>); sin/cos of the yaw are the double functions
+// rounded to float.
+__device__ __forceinline__ void make_rotation(float sr, float cr, float sp, float cp, float yaw, float r[9])
+{
+  double sd, cd;
+  sincos(static_cast<double>(yaw), &sd, &cd);
+  const float sy = __double2float_rn(sd), cy = __double2float_rn(cd);
+  r[0] = fmul(cy, cp);
+  r[1] = fsub(fmul(fmul(cy, sp), sr), fmul(sy, cr));
+  r[2] = fadd(fmul(fmul(cy, sp), cr), fmul(sy, sr));
+  r[3] = fmul(sy, cp);
+  r[4] = fadd(fmul(fmul(sy, sp), sr), fmul(cy, cr));
+  r[5] = fsub(fmul(fmul(sy, sp), cr), fmul(cy, sr));
+  r[6] = -sp;
+  r[7] = fmul(cp, sr);
+  r[8] = fmul(cp, cr);
+}
+
+__device__ __forceinline__ void make_partxf(const GridView& g, float sr, float cr, float sp, float cp, float tx,
+                                            float ty, float tz, float yaw, PartXf& p)
+{
+  make_rotation(sr, cr, sp, cp, yaw, p.r);
+  const float t[3] = { tx, ty, tz };
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+  {
+    const double off = __dsub_rn(static_cast<double>(t[a]), g.min[a]);  // Grid3d.cpp:155-157
+    p.off[a] = off;
+    p.H[a] = __double2float_rn(off);
+    p.L[a] = __double2float_rn(__dsub_rn(off, static_cast<double>(p.H[a])));
+  }
+}
+
+// Cell index along one axis for an exact X, -1 when the point is rejected.
+__device__ __forceinline__ int locate_axis(float X, const float* T, float V, float inv_res, uint32_t size)
+{
+  if (!(X >= 0.0f) || !(X < V))
+    return -1;
+  int k = __float2int_rz(fmul(X, inv_res));
+  k = min(k, static_cast<int>(size) - 1);
+  if (X < T[k])
+    k -= 1;
+  else if (X >= T[k + 1])
+    k += 1;
+  return k;
+}
+
+// True when a threshold lies within m of X (the estimate may then be on the wrong side).
+__device__ __forceinline__ bool near_threshold(float X, int k, const float* T, float V, float m)
+{
+  if (fabsf(X) <= m || fabsf(V - X) <= m)
+    return true;
+  if (k < 0)
+    return false;
+  return (X - T[k] <= m) || (T[k + 1] - X <= m);
+}
+
+// Transformed coordinate, estimated in float-float.  Sets *amb when the exact
+// rounding might classify differently.
+__device__ __forceinline__ float xform_axis(float s, float H, float L, float& m)
+{
+  const float a = fadd(s, H);
+  const float bv = fsub(a, s);
+  const float av = fsub(a, bv);
+  const float br = fsub(H, bv);
+  const float ar = fsub(s, av);
+  const float e = fadd(ar, br);
+  const float X = fadd(a, fadd(e, L));
+  // |X - exact| <= 1.25 ulp(X) + 2^-47 (|s| + |H|); the margin covers it with room.
+  m = fmul(fadd(fadd(fabsf(X), fabsf(H)), fabsf(s)), 2.384185791015625e-07f /* 2^-22 */);
+  return X;
+}
+
+// Grid cell index of scan point (px, py, pz0) for the particle, or -1 when the
+// reference skips the point.  pz0 is s.z + 0.0f (Grid3d.cpp:174-176).
+// `tab` points at the locate tables (in shared memory in the kernels).
+__device__ __forceinline__ int64_t cell_of_point(const GridView& g, const float* tab, const PartXf& p, float px,
+                                                 float py, float pz0)
+{
+  float s[3];
+  s[0] = fadd(fadd(fmul(px, p.r[0]), fmul(py, p.r[1])), fmul(pz0, p.r[2]));
+  s[1] = fadd(fadd(fmul(px, p.r[3]), fmul(py, p.r[4])), fmul(pz0, p.r[5]));
+  s[2] = fadd(fadd(fmul(px, p.r[6]), fmul(py, p.r[7])), fmul(pz0, p.r[8]));
+  int k[3];
+  bool amb = false;
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+  {
+    float m;
+    const float X = xform_axis(s[a], p.H[a], p.L[a], m);
+    const float* T = tab + g.toff[a];
+    k[a] = locate_axis(X, T, g.V[a], g.inv_res[a], g.size[a]);
+    amb |= near_threshold(X, k[a], T, g.V[a], m);
+  }
+  if (amb)
+  {
+    // Exact path: the reference's double add, rounded to float once more.
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+    {
+      const float X = __double2float_rn(__dadd_rn(static_cast<double>(s[a]), p.off[a]));
+      k[a] = locate_axis(X, tab + g.toff[a], g.V[a], g.inv_res[a], g.size[a]);
+    }
+  }
+  if (k[0] < 0 || k[1] < 0 || k[2] < 0)
+    return -1;
+  // uint32 index arithmetic of Grid3d.cpp:187
+  const uint32_t idx = static_cast<uint32_t>(k[0]) + static_cast<uint32_t>(k[1]) * g.step_y +
+                       static_cast<uint32_t>(k[2]) * g.step_z;
+  return static_cast<int64_t>(idx);
+}
+
+template <int STORAGE>
+__device__ __forceinline__ float gather_prob(const GridView& g, uint32_t idx)
+{
+  if (STORAGE == AMCL_GRID_F32)
+    return __ldg(g.prob_f32 + idx);
+  else if (STORAGE == AMCL_GRID_F16)
+    return __half2float(__ldg(g.prob_f16 + idx));
+  else
+    return fmul(static_cast<float>(__ldg(g.prob_u8 + idx)), g.u8_scale);
+}
+
+// isIntoMap (Grid3d.cpp:201-208) as exact float compares.
+__device__ __forceinline__ bool into_map(const GridView& g, float x, float y, float z)
+{
+  return g.built && x >= g.in_lo[0] && x < g.in_hi[0] && y >= g.in_lo[1] && y < g.in_hi[1] && z >= g.in_lo[2] &&
+         z < g.in_hi[2];
+}
+
+}  // namespace amcl

@@ -1,0 +1,520 @@
+// Per-particle scan-to-map likelihood: Grid3d::computeCloudWeight
+// (amcl3d/src/Grid3d.cpp:133-199) for every in-map particle, fused with the
+// range-beacon weight ParticleFilter::computeRangeWeight (ParticleFilter.cpp:224-244)
+// and with the exact sums of both weights over the in-map particles that the
+// normalisation of ParticleFilter::update needs (ParticleFilter.cpp:129-153).
+//
+// Two kernels compute the same bits:
+//  * fused: one thread per particle walks the whole cloud in cloud order (the
+//    scan is staged through shared memory as float4 chunks read by every thread of
+//    the block: a broadcast), gathering the cell probability and summing it in
+//    float in the reference's order.  Used when there are enough particles to fill
+//    the GPU.
+//  * two-phase: for few particles, phase 1 spreads (particle tile x point slice)
+//    blocks over every SM, each warp holding 32 particles (one per lane) and
+//    writing the gathered probability (or -1 for a skipped point) to a scratch
+//    slab laid out [tile][point][lane]; phase 2 gives each tile one warp that
+//    bulk-copies its slab through shared memory (cp.async.bulk on an mbarrier
+//    ring) and adds the values in cloud order, so the float sum is the same as the
+//    reference's running sum.
+#include "bulk.cuh"
+#include "exact.cuh"
+#include "grid.cuh"
+
+using namespace amcl;
+
+namespace
+{
+constexpr int WT_THREADS = 256;
+constexpr int WT_CHUNK = 1024;  // points staged per block iteration (16 KB)
+constexpr int MAX_RANGES = 64;
+
+__device__ __forceinline__ float exp_f32_via_f64(float x) { return __double2float_rn(exp(static_cast<double>(x))); }
+
+// ParticleFilter::computeRangeWeight (ParticleFilter.cpp:224-244), float overloads.
+__device__ __forceinline__ float range_weight(float x, float y, float z, const float4* rg, int nr, float k1, float k2)
+{
+  if (nr == 0)
+    return 0.0f;
+  float w = 1.0f;
+  for (int b = 0; b < nr; ++b)
+  {
+    const float4 R = rg[b];  // (r, ax, ay, az)
+    const float dx = fsub(x, R.y), dy = fsub(y, R.z), dz = fsub(z, R.w);
+    const float r = __fsqrt_rn(fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz)));
+    const float d = fsub(r, R.x);
+    const float e = exp_f32_via_f64(fmul(fmul(-k2, d), d));
+    w = fmul(w, fmul(k1, e));
+  }
+  return w;
+}
+
+// Block-wide exact sums of (a, b) added to the grid-wide digit accumulators.
+__device__ __forceinline__ void block_exact_pair(float va, float vb, bool take, unsigned long long* acc_a,
+                                                 unsigned long long* acc_b, X320* s_part)
+{
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  X320 xa = take ? x320_from_float(va) : x320_zero();
+  X320 xb = take ? x320_from_float(vb) : x320_zero();
+  xa = x320_warp_sum(xa);
+  xb = x320_warp_sum(xb);
+  if (lane == 0)
+  {
+    s_part[2 * wid] = xa;
+    s_part[2 * wid + 1] = xb;
+  }
+  __syncthreads();
+  if (wid == 0)
+  {
+    X320 ta = lane < nw ? s_part[2 * lane] : x320_zero();
+    X320 tb = lane < nw ? s_part[2 * lane + 1] : x320_zero();
+    ta = x320_warp_sum(ta);
+    tb = x320_warp_sum(tb);
+    if (lane == 0)
+    {
+      if (acc_a)
+        x320_atomic_add(acc_a, ta);
+      if (acc_b)
+        x320_atomic_add(acc_b, tb);
+    }
+  }
+}
+
+template <int STORAGE, int SUM>
+__global__ __launch_bounds__(WT_THREADS) void k_weight_fused(WeightArgs a, GridView g)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  float4* s_pts = reinterpret_cast<float4*>(smem);
+  float4* s_rg = s_pts + WT_CHUNK;
+  X320* s_part = reinterpret_cast<X320*>(s_rg + MAX_RANGES);
+  float* s_tab = reinterpret_cast<float*>(s_part + 2 * (WT_THREADS / 32));
+  const uint32_t ntab = g.size[0] + g.size[1] + g.size[2] + 3;
+  for (uint32_t i = threadIdx.x; i < ntab; i += blockDim.x)
+    s_tab[i] = g.T[i];
+  for (uint32_t i = threadIdx.x; i < a.nr; i += blockDim.x)
+    s_rg[i] = a.ranges[i];
+
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = p < a.P;
+  float4 pose = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (active)
+    pose = a.pose[p];
+  const bool inm = active && (a.ignore_map || into_map(g, pose.x, pose.y, pose.z));
+  PartXf xf;
+  if (inm)
+    make_partxf(g, a.sr, a.cr, a.sp, a.cp, pose.x, pose.y, pose.z, pose.w, xf);
+
+  float sum = 0.0f, comp = 0.0f;
+  int n = 0;
+  for (uint32_t base = 0; base < a.N; base += WT_CHUNK)
+  {
+    const uint32_t cnt = min(static_cast<uint32_t>(WT_CHUNK), a.N - base);
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x)
+    {
+      float4 c = a.cloud[base + i];
+      c.z = fadd(c.z, 0.0f);  // (point->z + error_z), error_z = 0 (Grid3d.cpp:166,174-176)
+      s_pts[i] = c;
+    }
+    __syncthreads();
+    if (!inm)
+      continue;
+    for (uint32_t k = 0; k < cnt; k += 8)
+    {
+      int64_t cell[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+      {
+        cell[j] = -1;
+        if (k + j < cnt)
+        {
+          const float4 s = s_pts[k + j];
+          cell[j] = cell_of_point(g, s_tab, xf, s.x, s.y, s.z);
+        }
+      }
+      float v[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        v[j] = cell[j] >= 0 ? gather_prob<STORAGE>(g, static_cast<uint32_t>(cell[j])) : 0.0f;
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+      {
+        if (cell[j] < 0)
+          continue;
+        if (SUM == 0)
+        {
+          sum = fadd(sum, v[j]);  // weight += grid_ptr[grid_index].prob (Grid3d.cpp:191)
+        }
+        else
+        {
+          const float t = fadd(sum, v[j]);
+          comp = fadd(comp, fabsf(sum) >= fabsf(v[j]) ? fadd(fsub(sum, t), v[j]) : fadd(fsub(v[j], t), sum));
+          sum = t;
+        }
+        n += 1;
+      }
+    }
+  }
+  float wpv = 0.0f, wrv = 0.0f;
+  if (inm)
+  {
+    const float tot = SUM == 0 ? sum : fadd(sum, comp);
+    wpv = (n <= 10) ? 0.0f : __fdiv_rn(tot, static_cast<float>(n));  // Grid3d.cpp:198
+    wrv = range_weight(pose.x, pose.y, pose.z, s_rg, static_cast<int>(a.nr), a.k1, a.k2);
+    a.wp[p] = wpv;
+    a.wr[p] = wrv;
+  }
+  if (active && a.inmap)
+    a.inmap[p] = inm ? 1 : 0;
+  if (a.acc_wp || a.acc_wr)
+  {
+    __syncthreads();
+    block_exact_pair(wpv, wrv, inm, a.acc_wp, a.acc_wr, s_part);
+  }
+}
+
+// ---- two-phase ----------------------------------------------------------------------------
+constexpr int TP_WARPS = 8;
+constexpr int TP_PTS_PER_WARP = 32;
+constexpr int TP_PTS_PER_BLOCK = TP_WARPS * TP_PTS_PER_WARP;
+
+struct __align__(16) PartRec
+{
+  PartXf xf;
+  int inm;
+};
+
+template <int STORAGE>
+__global__ __launch_bounds__(TP_WARPS * 32) void k_weight_tile_vals(WeightArgs a, GridView g)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  float4* s_pts = reinterpret_cast<float4*>(smem);
+  PartRec* s_rec = reinterpret_cast<PartRec*>(s_pts + TP_PTS_PER_BLOCK);
+  float* s_tab = reinterpret_cast<float*>(s_rec + 32);
+  const uint32_t ntab = g.size[0] + g.size[1] + g.size[2] + 3;
+  for (uint32_t i = threadIdx.x; i < ntab; i += blockDim.x)
+    s_tab[i] = g.T[i];
+  const uint32_t tile = blockIdx.x;
+  const uint32_t base = blockIdx.y * TP_PTS_PER_BLOCK;
+  const uint32_t cnt = base < a.N ? min(static_cast<uint32_t>(TP_PTS_PER_BLOCK), a.N - base) : 0u;
+  for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x)
+  {
+    float4 c = a.cloud[base + i];
+    c.z = fadd(c.z, 0.0f);
+    s_pts[i] = c;
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (wid == 0)
+  {
+    const uint32_t p = tile * 32 + lane;
+    PartRec r;
+    r.inm = 0;
+    if (p < a.P)
+    {
+      const float4 pose = a.pose[p];
+      r.inm = (a.ignore_map || into_map(g, pose.x, pose.y, pose.z)) ? 1 : 0;
+      if (r.inm)
+        make_partxf(g, a.sr, a.cr, a.sp, a.cp, pose.x, pose.y, pose.z, pose.w, r.xf);
+    }
+    s_rec[lane] = r;
+  }
+  __syncthreads();
+  const PartRec rec = s_rec[lane];
+  if (!rec.inm)
+    return;
+  float* out = a.scratch + (static_cast<uint64_t>(tile) * a.N) * 32 + lane;
+  const uint32_t k0 = wid * TP_PTS_PER_WARP;
+  for (uint32_t kk = 0; kk < TP_PTS_PER_WARP; kk += 8)
+  {
+    int64_t cell[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+    {
+      const uint32_t k = k0 + kk + j;
+      cell[j] = -2;
+      if (k < cnt)
+      {
+        const float4 s = s_pts[k];
+        cell[j] = cell_of_point(g, s_tab, rec.xf, s.x, s.y, s.z);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+    {
+      const uint32_t k = k0 + kk + j;
+      if (cell[j] == -2)
+        continue;
+      const float v = cell[j] >= 0 ? gather_prob<STORAGE>(g, static_cast<uint32_t>(cell[j])) : -1.0f;
+      out[static_cast<uint64_t>(base + k) * 32] = v;
+    }
+  }
+}
+
+constexpr int TR_STAGE_PTS = 128;  // points per stage: 128 x 32 lanes x 4 B = 16 KB
+constexpr int TR_STAGES = 4;
+
+template <int SUM>
+__global__ __launch_bounds__(32) void k_weight_tile_reduce(WeightArgs a, GridView g)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  float* s_buf = reinterpret_cast<float*>(smem);  // TR_STAGES x TR_STAGE_PTS x 32
+  __shared__ __align__(8) uint64_t s_bar[TR_STAGES];
+  __shared__ float4 s_rg[MAX_RANGES];
+  const int lane = threadIdx.x;
+  const uint32_t tile = blockIdx.x;
+  const uint32_t p = tile * 32 + lane;
+  for (uint32_t i = lane; i < a.nr; i += 32)
+    s_rg[i] = a.ranges[i];
+  float4 pose = make_float4(0.f, 0.f, 0.f, 0.f);
+  const bool active = p < a.P;
+  if (active)
+    pose = a.pose[p];
+  const bool inm = active && (a.ignore_map || into_map(g, pose.x, pose.y, pose.z));
+  const bool any = __any_sync(0xFFFFFFFFu, inm);
+  if (lane == 0)
+    for (int s = 0; s < TR_STAGES; ++s)
+      mbar_init(&s_bar[s], 1);
+  mbar_fence_init();
+  __syncwarp();
+  const float* slab = a.scratch + static_cast<uint64_t>(tile) * a.N * 32;
+  const uint32_t nst = (a.N + TR_STAGE_PTS - 1) / TR_STAGE_PTS;
+  float sum = 0.0f, comp = 0.0f;
+  int n = 0;
+  bool ok = true;
+  if (any && a.N)
+  {
+    if (lane == 0)
+      for (uint32_t st = 0; st < min(nst, static_cast<uint32_t>(TR_STAGES)); ++st)
+      {
+        const uint32_t pts = min(static_cast<uint32_t>(TR_STAGE_PTS), a.N - st * TR_STAGE_PTS);
+        mbar_arrive_expect_tx(&s_bar[st], pts * 128u);
+        bulk_g2s(s_buf + st * TR_STAGE_PTS * 32, slab + static_cast<uint64_t>(st) * TR_STAGE_PTS * 32, pts * 128u,
+                 &s_bar[st]);
+      }
+    for (uint32_t st = 0; st < nst; ++st)
+    {
+      const int slot = st % TR_STAGES;
+      const uint32_t parity = (st / TR_STAGES) & 1u;
+      if (!mbar_wait_bounded(&s_bar[slot], parity, a.err))
+      {
+        ok = false;
+        break;
+      }
+      const uint32_t pts = min(static_cast<uint32_t>(TR_STAGE_PTS), a.N - st * TR_STAGE_PTS);
+      const float* buf = s_buf + slot * TR_STAGE_PTS * 32;
+      if (inm)
+      {
+        for (uint32_t k = 0; k < pts; ++k)
+        {
+          const float v = buf[k * 32 + lane];
+          if (v < 0.0f)
+            continue;
+          if (SUM == 0)
+          {
+            sum = fadd(sum, v);
+          }
+          else
+          {
+            const float t = fadd(sum, v);
+            comp = fadd(comp, fabsf(sum) >= fabsf(v) ? fadd(fsub(sum, t), v) : fadd(fsub(v, t), sum));
+            sum = t;
+          }
+          n += 1;
+        }
+      }
+      __syncwarp();
+      const uint32_t nxt = st + TR_STAGES;
+      if (lane == 0 && nxt < nst)
+      {
+        const uint32_t np = min(static_cast<uint32_t>(TR_STAGE_PTS), a.N - nxt * TR_STAGE_PTS);
+        mbar_arrive_expect_tx(&s_bar[slot], np * 128u);
+        bulk_g2s(s_buf + slot * TR_STAGE_PTS * 32, slab + static_cast<uint64_t>(nxt) * TR_STAGE_PTS * 32, np * 128u,
+                 &s_bar[slot]);
+      }
+    }
+    if (!ok)
+    {
+      // Drain whatever is still in flight (bounded) before leaving.
+      for (uint32_t st = 0; st < min(nst, static_cast<uint32_t>(TR_STAGES)); ++st)
+        mbar_wait_bounded(&s_bar[st], 0, nullptr);
+    }
+  }
+  float wpv = 0.0f, wrv = 0.0f;
+  if (inm && ok)
+  {
+    const float tot = SUM == 0 ? sum : fadd(sum, comp);
+    wpv = (n <= 10) ? 0.0f : __fdiv_rn(tot, static_cast<float>(n));
+    wrv = range_weight(pose.x, pose.y, pose.z, s_rg, static_cast<int>(a.nr), a.k1, a.k2);
+    a.wp[p] = wpv;
+    a.wr[p] = wrv;
+  }
+  if (active && a.inmap)
+    a.inmap[p] = inm ? 1 : 0;
+  X320 xa = (inm && ok) ? x320_from_float(wpv) : x320_zero();
+  X320 xb = (inm && ok) ? x320_from_float(wrv) : x320_zero();
+  xa = x320_warp_sum(xa);
+  xb = x320_warp_sum(xb);
+  if (lane == 0)
+  {
+    if (a.acc_wp)
+      x320_atomic_add(a.acc_wp, xa);
+    if (a.acc_wr)
+      x320_atomic_add(a.acc_wr, xb);
+  }
+}
+
+template <int STORAGE, int SUM>
+int launch_fused(const WeightArgs& a, const GridView& g, cudaStream_t s)
+{
+  const size_t smem = WT_CHUNK * sizeof(float4) + MAX_RANGES * sizeof(float4) + 2 * (WT_THREADS / 32) * sizeof(X320) +
+                      (g.size[0] + g.size[1] + g.size[2] + 3) * sizeof(float);
+  static bool attr_done = false;
+  if (!attr_done)
+  {
+    cudaFuncSetAttribute(k_weight_fused<STORAGE, SUM>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr_done = true;
+  }
+  k_weight_fused<STORAGE, SUM><<<ceil_div(a.P, WT_THREADS), WT_THREADS, smem, s>>>(a, g);
+  AMCL_LAUNCH_CHECK("k_weight_fused");
+  return AMCL_OK;
+}
+
+template <int STORAGE, int SUM>
+int launch_two_phase(const WeightArgs& a, const GridView& g, cudaStream_t s)
+{
+  const size_t smem1 = TP_PTS_PER_BLOCK * sizeof(float4) + 32 * sizeof(PartRec) +
+                       (g.size[0] + g.size[1] + g.size[2] + 3) * sizeof(float);
+  const size_t smem2 = static_cast<size_t>(TR_STAGES) * TR_STAGE_PTS * 32 * sizeof(float);
+  static bool attr_done = false;
+  if (!attr_done)
+  {
+    cudaFuncSetAttribute(k_weight_tile_vals<STORAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_weight_tile_reduce<SUM>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr_done = true;
+  }
+  const unsigned tiles = ceil_div(a.P, 32);
+  if (a.N)
+  {
+    dim3 grid1(tiles, ceil_div(a.N, TP_PTS_PER_BLOCK));
+    k_weight_tile_vals<STORAGE><<<grid1, TP_WARPS * 32, smem1, s>>>(a, g);
+    AMCL_LAUNCH_CHECK("k_weight_tile_vals");
+  }
+  k_weight_tile_reduce<SUM><<<tiles, 32, smem2, s>>>(a, g);
+  AMCL_LAUNCH_CHECK("k_weight_tile_reduce");
+  return AMCL_OK;
+}
+
+template <int STORAGE>
+int launch_storage(const WeightArgs& a, const GridView& g, cudaStream_t s)
+{
+  const bool tp = a.kernel == 2;
+  if (a.cloud_sum == 0)
+    return tp ? launch_two_phase<STORAGE, 0>(a, g, s) : launch_fused<STORAGE, 0>(a, g, s);
+  return tp ? launch_two_phase<STORAGE, 1>(a, g, s) : launch_fused<STORAGE, 1>(a, g, s);
+}
+}  // namespace
+
+namespace amcl
+{
+uint64_t two_phase_scratch_floats(uint32_t P, uint32_t N)
+{
+  return static_cast<uint64_t>(ceil_div(P, 32)) * 32ull * N;
+}
+
+int choose_weight_kernel(uint32_t P, uint32_t N)
+{
+  // Fused when one thread per particle already gives every SM several warps.
+  const uint64_t warps = ceil_div(P, 32);
+  if (warps >= 8ull * static_cast<uint64_t>(device_sm_count()))
+    return 1;
+  if (two_phase_scratch_floats(P, N) * 4ull > (1ull << 30))
+    return 1;
+  return 2;
+}
+
+void pack_cloud(const float* xyz, uint32_t n, uint32_t stride, float4* out)
+{
+  for (uint32_t i = 0; i < n; ++i)
+    out[i] = make_float4(xyz[static_cast<uint64_t>(i) * stride], xyz[static_cast<uint64_t>(i) * stride + 1],
+                         xyz[static_cast<uint64_t>(i) * stride + 2], 0.0f);
+}
+
+int launch_cloud_weight(amcl_grid_s* g, const WeightArgs& a, cudaStream_t s)
+{
+  if (a.nr > MAX_RANGES)
+    return fail(AMCL_ERANGE, "update: more than 64 range measurements");
+  if (a.P == 0)
+    return AMCL_OK;
+  if (a.kernel == 2 && (!a.scratch || a.scratch_floats < two_phase_scratch_floats(a.P, a.N)))
+    return fail(AMCL_EINVAL, "two-phase weighting without a large enough scratch buffer");
+  switch (g->view.storage)
+  {
+    case AMCL_GRID_F16:
+      return launch_storage<AMCL_GRID_F16>(a, g->view, s);
+    case AMCL_GRID_U8:
+      return launch_storage<AMCL_GRID_U8>(a, g->view, s);
+    default:
+      return launch_storage<AMCL_GRID_F32>(a, g->view, s);
+  }
+}
+}  // namespace amcl
+
+// ---- batch of Grid3d::computeCloudWeight calls ---------------------------------------------
+
+extern "C" int amcl_grid_cloud_weights(amcl_grid_t g, const float* poses4, uint32_t P, const float* xyz, uint32_t n,
+                                       uint32_t stride_floats, float roll, float pitch, float* out)
+{
+  if (!g || (P && (!poses4 || !out)) || (n && !xyz) || stride_floats < 3)
+    return fail(AMCL_EINVAL, "amcl_grid_cloud_weights: bad arguments");
+  if (!P)
+    return AMCL_OK;
+  if (!g->built)
+  {
+    for (uint32_t i = 0; i < P; ++i)
+      out[i] = 0.0f;  // Grid3d.cpp:136-137
+    return AMCL_OK;
+  }
+  cudaStream_t s = g->st.s;
+  DevBuf d_pose, d_cloud, d_wp, d_wr, d_scratch, d_err;
+  int rc;
+  if ((rc = d_pose.ensure(P * 16ull)) || (rc = d_cloud.ensure(std::max<uint64_t>(n, 1) * 16)) ||
+      (rc = d_wp.ensure(P * 4ull)) || (rc = d_wr.ensure(P * 4ull)) || (rc = d_err.ensure(4)))
+    return rc;
+  std::vector<float4> hc(n);
+  pack_cloud(xyz, n, stride_floats, hc.data());
+  AMCL_CUDA_TRY(cudaMemcpyAsync(d_pose.p, poses4, P * 16ull, cudaMemcpyHostToDevice, s));
+  if (n)
+    AMCL_CUDA_TRY(cudaMemcpyAsync(d_cloud.p, hc.data(), n * 16ull, cudaMemcpyHostToDevice, s));
+  AMCL_CUDA_TRY(cudaMemsetAsync(d_err.p, 0, 4, s));
+  WeightArgs a{};
+  a.pose = d_pose.as<float4>();
+  a.P = P;
+  a.cloud = d_cloud.as<float4>();
+  a.N = n;
+  a.sr = sinf(roll);
+  a.cr = cosf(roll);
+  a.sp = sinf(pitch);
+  a.cp = cosf(pitch);
+  a.wp = d_wp.as<float>();
+  a.wr = d_wr.as<float>();
+  a.err = d_err.as<int>();
+  a.ignore_map = 1;
+  a.kernel = choose_weight_kernel(P, n);
+  if (a.kernel == 2)
+  {
+    if ((rc = d_scratch.ensure(two_phase_scratch_floats(P, n) * 4)))
+      return rc;
+    a.scratch = d_scratch.as<float>();
+    a.scratch_floats = d_scratch.bytes / 4;
+  }
+  grid_apply_l2_window(g, s);
+  if ((rc = launch_cloud_weight(g, a, s)))
+    return rc;
+  int e = 0;
+  AMCL_CUDA_TRY(cudaMemcpyAsync(out, d_wp.p, P * 4ull, cudaMemcpyDeviceToHost, s));
+  AMCL_CUDA_TRY(cudaMemcpyAsync(&e, d_err.p, 4, cudaMemcpyDeviceToHost, s));
+  AMCL_CUDA_TRY(cudaStreamSynchronize(s));
+  if (e)
+    return fail(AMCL_ETIMEDOUT, "amcl_grid_cloud_weights: a bounded device-side wait gave up");
+  return AMCL_OK;
+}

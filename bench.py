@@ -1,0 +1,413 @@
+#!/usr/bin/env python
+"""Benchmark of the amcl3d particle-filter hot path on GB300.
+
+One step = predict + update (cloud weights, range weights, blend, normalise, mean)
++ getMean + resample of one filter over one synthetic scan, the sequence the ROS
+node runs per accepted scan (Node.cpp:154-182).  Metric: particle x point weights
+per second (P * N per step / step time), whole job.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--config warehouse|room]
+                  [--impl ours|reference]
+
+`value` times the steps with the scan already resident in HBM (CUDA events on the
+filter's stream); `e2e` times the same steps through the C ABI with host buffers
+(the scan copied host->device and the mean read back every step).  The default
+workload is the large single-filter configuration (2000x2000x400-cell warehouse,
+200k particles, 20k points); `room` is the CPU-runnable 400x400x100 case.
+Multi-GPU runs are independent replicas (one filter per GPU, no collective on the
+data path), launched one process per GPU by torchrun.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+CONFIGS = {
+    "room": dict(
+        workload="plain single filter: 20x20x5 m room at 0.05 m (400x400x100 cells), 40 cuboids 0.3-3 m, "
+                 "600 particles, 1000-point scan (32x32 beams, 15 m), 3 beacons, alpha 0.5",
+        size_m=(20.0, 20.0, 5.0), n_boxes=40, box_range=(0.3, 3.0), max_box_height=None, P=600, n_elev=32,
+        n_azim=32, max_range=15.0, N=1000, B=3, elev=(-25.0, 25.0)),
+    "warehouse": dict(
+        workload="large single filter: 100x100x20 m warehouse at 0.05 m (2000x2000x400 cells, FP32 grid), "
+                 "2000 cuboid shelves/pillars, 200000 particles, 20000-point scan (64x312 beams, 40 m), "
+                 "6 beacons, alpha 0.5",
+        size_m=(100.0, 100.0, 20.0), n_boxes=2000, box_range=(0.3, 3.0), max_box_height=8.0, P=200000, n_elev=64,
+        n_azim=312, max_range=40.0, N=20000, B=6, elev=(-20.0, 20.0)),
+}
+METRIC = "particle x point weights/s"
+UNIT = "weights/s"
+N_SCANS = 4
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ---- workload ------------------------------------------------------------------------------------
+
+def make_workload(cfg: dict, seed: int):
+    from amcl3d_gb300 import synth as S
+
+    t0 = time.perf_counter()
+    m = S.make_map(seed, size_m=cfg["size_m"], res=0.05, n_boxes=cfg["n_boxes"], box_range=cfg["box_range"],
+                   max_box_height=cfg["max_box_height"])
+    pose = S.free_pose(m, seed + 1)
+    scans, poses, odos = [], [], []
+    p = pose.copy()
+    for k in range(N_SCANS):
+        s = S.ray_cast(m, p, n_elev=cfg["n_elev"], n_azim=cfg["n_azim"], elev_deg=cfg["elev"],
+                       max_range=cfg["max_range"], n_max=cfg["N"], seed=seed + 10 + k)
+        scans.append(s)
+        poses.append(p.copy())
+        d = S.odometry_step(seed + 100 + k)
+        odos.append(d)
+        p = p + np.array([math.cos(p[3]) * 0.02, math.sin(p[3]) * 0.02, 0.0, 0.0])
+    parts = S.particles_around(pose, cfg["P"], seed + 2)
+    ranges = [S.beacons(m, q, cfg["B"], seed=seed + 200 + k) for k, q in enumerate(poses)]
+    occ_points = m.points
+    info = dict(min=m.min, max=m.max, res=m.res, dims=m.dims, n_points=int(occ_points.shape[0]))
+    del m
+    log(f"workload generated in {time.perf_counter() - t0:.1f}s: {info['n_points']} occupied voxels, "
+        f"scan sizes {[s.shape[0] for s in scans]}")
+    return occ_points, info, scans, ranges, odos, parts
+
+
+# ---- clocks sampled during the timed region --------------------------------------------------------
+
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---- CPU baseline: the oracle's restatement of the reference, on host threads --------------------
+
+def cpu_baseline(occ_points, info, scans, ranges, parts, seconds: float, threads: int | None = None,
+                 gpu_grid=None):
+    """Times the reference's update arithmetic (oracle restatement, float running
+    sums, libm trig/exp) on a particle sample, all host cores.  Returns (rate, desc)."""
+    import oracle as O
+
+    threads = threads or os.cpu_count() or 1
+    size = info["dims"]
+    if gpu_grid is not None:
+        d, p = gpu_grid.read_cells()
+    else:
+        d, p = O.compute_grid(occ_points, info["min"], info["max"], info["res"], 0.05, exp_mode=0)
+    g = O.GridData(info["min"], info["max"], info["res"], size, p.ravel(), d.ravel())
+    del d
+    scan = scans[0]
+    N = scan.shape[0]
+
+    def run(sample: np.ndarray):
+        chunks = np.array_split(sample, threads)
+        with ThreadPoolExecutor(threads) as ex:
+            list(ex.map(lambda c: O.update_f32(c, g, scan, ranges[0], 0.5, 0.1, 0.0, 0.0, yaw_trig=0, exp_mode=0)
+                        if len(c) else None, chunks))
+
+    # calibrate on a small sample, then size the timed sample to ~`seconds`
+    cal = parts[: max(threads * 4, 64)]
+    t0 = time.perf_counter()
+    run(cal)
+    dt = max(time.perf_counter() - t0, 1e-4)
+    rate = cal.shape[0] * N / dt
+    n_sample = int(min(parts.shape[0], max(threads * 8, rate * seconds / N)))
+    sample = parts[:n_sample]
+    t0 = time.perf_counter()
+    run(sample)
+    dt = time.perf_counter() - t0
+    return n_sample * N / dt, {
+        "cores": threads,
+        "kind": "port",
+        "sample": f"{n_sample} of {parts.shape[0]} particles x {N} points, one update "
+                  f"(C restatement of ParticleFilter::update with float running sums), {dt:.1f}s",
+    }
+
+
+# ---- our arm -----------------------------------------------------------------------------------
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic(workload_key: str):
+    p = ROOT / "profiles" / "traffic.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        v = d.get(workload_key, {}).get("cloud_weight_bytes_per_launch")
+        return v
+    return None
+
+
+def run_ours(args, cfg, rank, world, local_rank):
+    import torch
+
+    import amcl3d_gb300 as A
+    from amcl3d_gb300 import _native
+    from amcl3d_gb300 import synth as S
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    seed = 1000 + rank
+    occ_points, info, scans, ranges, odos, parts = make_workload(cfg, seed)
+    G = A.Grid3d()
+    t0 = time.perf_counter()
+    G.buildGridMap(occ_points, info["min"], info["max"], info["res"], S.SENSOR_DEV)
+    build_s = time.perf_counter() - t0
+    log(f"[rank {rank}] grid {info['dims']} built on the GPU in {build_s:.2f}s")
+
+    pf = A.ParticleFilter(seed=seed)
+    pf.set_particles(parts)
+    stream = torch.cuda.ExternalStream(pf.stream(), device=dev)
+    d_scans = [torch.from_numpy(np.ascontiguousarray(s)).to(dev) for s in scans]
+    torch.cuda.synchronize()
+    P, N = cfg["P"], cfg["N"]
+    l2_small = info["dims"][0] * info["dims"][1] * info["dims"][2] * 4 < 200 * 2**20
+    flush = torch.empty(512 * 2**20, dtype=torch.uint8, device=dev) if l2_small else None
+    import ctypes as C
+
+    def step(k, resident=True):
+        i = k % N_SCANS
+        pf.predict(*S.ODOM_MODS, *odos[i])
+        if resident:
+            rg = np.ascontiguousarray(ranges[i])
+            _native.call("amcl_pf_update_dev", pf.handle, G.handle, C.c_void_p(d_scans[i].data_ptr()),
+                         scans[i].shape[0], _native.fptr(rg), rg.shape[0], 0.5, 0.1, 0.0, 0.0)
+        else:
+            pf.update(G, scans[i], ranges[i], 0.5, 0.1, 0.0, 0.0)
+        pf.getMean()
+        pf.resample()
+
+    for k in range(args.warmup):
+        step(k)
+    torch.cuda.synchronize()
+    pf.profile(True)
+    pf.profile_read(reset=True)
+    launches0 = _native.kernel_launches()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    weights = 0
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clocks:
+        for k in range(args.steps):
+            if flush is not None:
+                with torch.cuda.stream(stream):
+                    flush.fill_(k & 0xFF)
+            with torch.cuda.stream(stream):
+                ev[k][0].record(stream)
+            step(args.warmup + k)
+            with torch.cuda.stream(stream):
+                ev[k][1].record(stream)
+            weights += P * scans[(args.warmup + k) % N_SCANS].shape[0]
+        torch.cuda.synchronize()
+    barrier(world)
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    gpu_launches = _native.kernel_launches() - launches0
+    prof = pf.profile_read(reset=True)
+    pf.profile(False)
+    ms_max = allreduce_max(ms, world, dev)
+    total_weights = allreduce_sum(weights, world, dev)
+    value = total_weights / (ms_max / 1e3)
+
+    # e2e: host scan per step through the C ABI, mean read back every step
+    for k in range(min(args.warmup, 2)):
+        step(k, resident=False)
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    e2e_weights = 0
+    for k in range(args.steps):
+        step(args.warmup + k, resident=False)
+        e2e_weights += P * scans[(args.warmup + k) % N_SCANS].shape[0]
+    torch.cuda.synchronize()
+    e2e_s = allreduce_max(time.perf_counter() - t0, world, dev)
+    e2e_total = allreduce_sum(e2e_weights, world, dev)
+    h2d = int(np.mean([s.shape[0] for s in scans]) * 16 + cfg["B"] * 16)
+    d2h = 4 + 120  # status word + the mean/variance record
+
+    cw_ms, cw_n = prof["cloud_weight"]
+    peak, peak_kind = load_peaks()
+    N_mean = float(np.mean([s.shape[0] for s in scans]))
+    alg_bytes = P * N_mean * 4 + 28 * P + 16 * N_mean + 16 * cfg["B"] * P
+    achieved = alg_bytes / (cw_ms / cw_n / 1e3) / 1e9 if cw_n else None
+    res = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded room/warehouse maps, ray-cast scans; no public dataset)",
+        "config": {"workload": cfg["workload"], "particles": P, "points": int(N_mean), "grid_cells":
+                   int(np.prod(info["dims"])), "beacons": cfg["B"], "parallelism": f"replicas x{world}",
+                   "l2": "flushed between steps (512 MB write)" if l2_small else
+                         "grid larger than L2 (6.4 GB FP32)", "grid_build_s": round(build_s, 3)},
+        "e2e": {"value": e2e_total / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(gpu_launches),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": load_traffic(args.config),
+                     "peak_source": peak_kind, "kernel": "cloud weight (per-particle scan gather)",
+                     "kernel_ms_per_launch": (cw_ms / cw_n) if cw_n else None,
+                     "algorithmic_bytes_per_launch": alg_bytes},
+        "kernel_ms": {k: (v[0] / v[1] if v[1] else None) for k, v in prof.items()},
+    }
+    res["clocks"] = clocks.summary()
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        rate, desc = cpu_baseline(occ_points, info, scans, ranges, parts, seconds=args.cpu_seconds, gpu_grid=G)
+        res["cpu_baseline"] = {"value": rate, "unit": UNIT, **desc}
+    return res
+
+
+def run_reference(args, cfg, rank, world):
+    """The reference's CPU path (its arithmetic, restated in C: the reference tree
+    cannot travel to this host) on all host cores, a bounded sample per step."""
+    if rank != 0:
+        return None
+    occ_points, info, scans, ranges, odos, parts = make_workload(cfg, 1000)
+    rates = []
+    desc = None
+    for k in range(args.warmup + args.steps):
+        rate, desc = cpu_baseline(occ_points, info, scans, ranges, parts, seconds=args.cpu_seconds / 4)
+        if k >= args.warmup:
+            rates.append(rate)
+    value = float(np.mean(rates))
+    return {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": cfg["workload"], "particles": cfg["P"], "points": cfg["N"]},
+        "cpu_baseline": {"value": value, "unit": UNIT, **desc},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+# ---- distributed helpers ------------------------------------------------------------------------------
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def allreduce_max(v, world, dev):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(v)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allreduce_sum(v, world, dev):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(v)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", choices=sorted(CONFIGS), default="warehouse")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    cfg = CONFIGS[args.config]
+    if args.impl == "reference":
+        res = run_reference(args, cfg, rank, world)
+        if rank == 0 and res:
+            print(json.dumps(res), flush=True)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    res = run_ours(args, cfg, rank, world, local_rank)
+    if rank == 0:
+        print(json.dumps(res), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,230 @@
+/*
+ * amcl3d_gpu.h - C ABI of the GB300 particle-filter hot path of amcl3d.
+ *
+ * Two opaque handles mirror the two classes of the amcl3d filter core:
+ *   amcl_grid_t  <->  amcl3d::Grid3d         (amcl3d/src/Grid3d.h:34-159)
+ *   amcl_pf_t    <->  amcl3d::ParticleFilter (amcl3d/src/ParticleFilter.h:67-213)
+ * Every entry point returns an int status (AMCL_OK on success); amcl_last_error()
+ * gives the detail of the last failure on the calling thread.  Plain pointers and
+ * sizes only: no C++ or CUDA types cross this boundary (streams are passed as
+ * void*, a cudaStream_t or NULL for a stream the library creates).
+ *
+ * Host arrays are copied to the device inside the call; *_dev variants take
+ * device pointers for callers whose inputs are already resident in HBM.
+ * Calls on one handle are ordered on that handle's stream; entry points that
+ * return values to the host synchronise that stream.  A handle must not be used
+ * from two threads at once.
+ */
+#ifndef AMCL3D_GPU_H
+#define AMCL3D_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------ */
+enum
+{
+  AMCL_OK = 0,
+  AMCL_EINVAL = 1,    /* bad argument (null handle, size out of range, ...)        */
+  AMCL_ENOMEM = 2,    /* device or pinned-host allocation failed                   */
+  AMCL_ECUDA = 3,     /* a CUDA runtime call failed                                */
+  AMCL_ETIMEDOUT = 4, /* a bounded device-side wait gave up                        */
+  AMCL_ESTATE = 5,    /* call not valid in the handle's state (e.g. no grid yet)   */
+  AMCL_EIO = 6,       /* file could not be read or written                         */
+  AMCL_ERANGE = 7,    /* input exceeds a documented limit                          */
+  AMCL_ENOTSUP = 8    /* option not supported for this handle                      */
+};
+
+const char* amcl_status_string(int status);
+const char* amcl_last_error(void);
+int amcl_version(int* major, int* minor);
+
+/* ---- grid storage of the gathered per-cell probability -------------------------- */
+enum
+{
+  AMCL_GRID_F32 = 0, /* float, what the reference stores in Grid3dCell::prob          */
+  AMCL_GRID_F16 = 1, /* IEEE half                                                     */
+  AMCL_GRID_U8 = 2   /* uint8 code q, prob = q * scale, scale = max(prob) / 255        */
+};
+
+typedef struct amcl_grid_s* amcl_grid_t;
+typedef struct amcl_pf_s* amcl_pf_t;
+
+/* Mirrors PointCloudInfo's bounds/resolution (PointCloudTools.h:54-68) and
+ * Grid3dInfo's sizes (PointCloudTools.h:37-50). */
+typedef struct
+{
+  double min[3];     /* octo_min_x/y/z                                               */
+  double max[3];     /* octo_max_x/y/z                                               */
+  double resolution; /* octo_resol                                                   */
+  double sensor_dev; /* Grid3dInfo::sensor_dev                                       */
+  uint32_t size[3];  /* size_x, size_y, size_z = ceil((max - min) / resolution)      */
+  uint32_t storage;  /* AMCL_GRID_* currently used by the weighting kernels          */
+  float u8_scale;    /* scale of the uint8 storage (0 if not built)                  */
+  uint32_t reserved;
+} amcl_grid_info;
+
+/* ---- Grid3d --------------------------------------------------------------------- */
+
+/* Creates an empty grid bound to `stream` (NULL: the library creates one). */
+int amcl_grid_create(amcl_grid_t* out, void* stream);
+int amcl_grid_destroy(amcl_grid_t g);
+
+/* computeGrid (PointCloudTools.cpp:84-149), reached through Grid3d::open
+ * (Grid3d.cpp:25-78), spec alias buildGridMap: builds the nearest-occupied
+ * squared-distance field and its probability c1*expf(-d2*d2*c2) on the device from
+ * the occupied-leaf centres `xyz` (n points, `stride_floats` floats apart) and the
+ * octomap bounds.  The reference refuses more than 250e6 cells
+ * (PointCloudTools.cpp:103-105); this build accepts up to 2^32-1 cells (the limit of
+ * the reference's uint32 cell index, Grid3d.cpp:187) and returns AMCL_ERANGE above. */
+int amcl_grid_build(amcl_grid_t g, const float* xyz, uint64_t n, uint32_t stride_floats, const double min[3],
+                    const double max[3], double resolution, double sensor_dev);
+
+/* Loads cells computed elsewhere (host arrays of size_x*size_y*size_z floats; dist
+ * may be NULL).  The sizes in `info` must equal ceil((max-min)/res) per axis. */
+int amcl_grid_load_cells(amcl_grid_t g, const amcl_grid_info* info, const float* dist, const float* prob);
+
+/* The reference's .grid cache (Grid3d::saveGrid/loadGrid, Grid3d.cpp:210-275):
+ * uint32 size_x,size_y,size_z; double sensor_dev; {float dist, float prob}[cells].
+ * load rejects a sensor_dev that differs by >= DBL_EPSILON (Grid3d.cpp:256-260,
+ * returns AMCL_ESTATE) and a file whose sizes do not match the bounds. */
+int amcl_grid_save(amcl_grid_t g, const char* path);
+int amcl_grid_load(amcl_grid_t g, const char* path, const double min[3], const double max[3], double resolution,
+                   double sensor_dev);
+
+int amcl_grid_info_get(amcl_grid_t g, amcl_grid_info* out);
+/* Copies cells [first, first+count) to host arrays (either may be NULL). */
+int amcl_grid_read_cells(amcl_grid_t g, uint64_t first, uint64_t count, float* dist, float* prob);
+
+/* Selects the storage the weighting kernels gather (building F16/U8 copies from the
+ * F32 probabilities on first use). */
+int amcl_grid_set_storage(amcl_grid_t g, int storage);
+
+/* Keeps the gathered probability array in an L2 persisting access-policy window on
+ * this grid's stream and on the streams of filters that use it (0 = off, default). */
+int amcl_grid_set_l2_window(amcl_grid_t g, int enable);
+
+/* Grid3d::isIntoMap (Grid3d.cpp:201-208): min <= p < max per axis, 0 if not built. */
+int amcl_grid_is_into_map(amcl_grid_t g, float x, float y, float z, int* inside);
+
+/* Grid3d::computeCloudWeight (Grid3d.cpp:133-199) for P poses (x, y, z, yaw as 4
+ * floats each) and one host cloud (n points, stride_floats apart) at shared roll and
+ * pitch.  out[p] is the mean probability of the in-grid points, 0 if 10 or fewer
+ * points fall inside the grid (and 0 for every pose when no grid is built). */
+int amcl_grid_cloud_weights(amcl_grid_t g, const float* poses4, uint32_t P, const float* xyz, uint32_t n,
+                            uint32_t stride_floats, float roll, float pitch, float* out);
+
+/* Grid3d::buildGridSliceMsg (Grid3d.cpp:80-121): int8 occupancy of the z slice,
+ * prob scaled to 0..100 by the slice maximum.  Writes min(cap, len) values; *len,
+ * *width, *height receive the message sizes.  AMCL_EINVAL when z is outside the map. */
+int amcl_grid_slice(amcl_grid_t g, double z, int8_t* out, uint64_t cap, uint64_t* len, uint32_t* width,
+                    uint32_t* height);
+
+/* ---- ParticleFilter ----------------------------------------------------------------
+ * Particles are exchanged as amcl3d::Particle, 7 floats each in this order:
+ * x, y, z, a (yaw), w, wp, wr (ParticleFilter.h:35-49). */
+
+int amcl_pf_create(amcl_pf_t* out, uint64_t seed, void* stream);
+int amcl_pf_destroy(amcl_pf_t pf);
+
+/* ParticleFilter::init (ParticleFilter.cpp:46-95), spec alias
+ * buildParticlesPool: |num_particles| particles, particle 0 at the given pose, the
+ * rest drawn from N(pose, dev) per axis; weights c1*exp(-d^2*c2) with
+ * dev = max(x_dev, y_dev, z_dev), normalised; the mean is computed. */
+int amcl_pf_init(amcl_pf_t pf, int num_particles, float x, float y, float z, float a, float x_dev, float y_dev,
+                 float z_dev, float a_dev);
+
+/* ParticleFilter::predict (ParticleFilter.cpp:97-119). */
+int amcl_pf_predict(amcl_pf_t pf, double odom_x_mod, double odom_y_mod, double odom_z_mod, double odom_a_mod,
+                    double delta_x, double delta_y, double delta_z, double delta_a);
+
+/* ParticleFilter::update (ParticleFilter.cpp:121-196) with a host cloud (n points,
+ * stride_floats apart; PCL's PointXYZ is 4 floats) and nr ranges given as
+ * (r, ax, ay, az) float quadruples (ParticleFilter.h:53-63). */
+int amcl_pf_update(amcl_pf_t pf, amcl_grid_t g, const float* xyz, uint32_t n, uint32_t stride_floats,
+                   const float* ranges4, uint32_t nr, double alpha, double sigma, double roll, double pitch);
+
+/* Same, with the cloud already on the device as n float4 (x, y, z, unused),
+ * 16-byte aligned, and the ranges on the host.  The cloud must stay valid until the
+ * next call that synchronises this filter's stream. */
+int amcl_pf_update_dev(amcl_pf_t pf, amcl_grid_t g, const void* cloud_f4_dev, uint32_t n, const float* ranges4,
+                       uint32_t nr, double alpha, double sigma, double roll, double pitch);
+
+/* Range-only update declared at ParticleFilter.h:157 but never defined by the
+ * reference: wr from the beacons only, wp = 0, w = (1 - alpha) * wr normalised. */
+int amcl_pf_update_ranges(amcl_pf_t pf, const float* ranges4, uint32_t nr, double alpha, double sigma);
+
+/* ParticleFilter::resample (ParticleFilter.cpp:198-222), systematic: the uniform
+ * draw comes from this filter's counter-based generator. */
+int amcl_pf_resample(amcl_pf_t pf);
+/* Same with the uniform draw u01 in [0, 1) given by the caller (r = u01 / N). */
+int amcl_pf_resample_with(amcl_pf_t pf, float u01);
+
+/* ParticleFilter::getMean (ParticleFilter.h:94-97): the mean stored by the last
+ * init/update as a Particle (7 floats; w, wp, wr are 0).  If mean_var is not NULL it
+ * receives the double mean x, y, z, a then the weighted variance x, y, z, a. */
+int amcl_pf_get_mean(amcl_pf_t pf, float mean7[7], double mean_var[8]);
+
+int amcl_pf_is_initialized(amcl_pf_t pf, int* initialized);
+int amcl_pf_size(amcl_pf_t pf, uint32_t* n);
+/* Copies min(cap, size) particles out / replaces the particle set (parity injection). */
+int amcl_pf_get_particles(amcl_pf_t pf, float* p7, uint32_t cap);
+int amcl_pf_set_particles(amcl_pf_t pf, const float* p7, uint32_t n);
+
+/* Options (amcl_pf_set_option). */
+enum
+{
+  /* Sum of the per-point probabilities inside a particle's weight:
+   * 0 = float running sum in cloud order (the reference's arithmetic, bit-exact),
+   * 1 = compensated (Neumaier) float sum in cloud order. */
+  AMCL_OPT_CLOUD_SUM = 1,
+  /* Cumulative weights driving resample:
+   * 0 = exact (fixed-point, equal to the correctly rounded real prefix),
+   * 1 = float running sum in particle order (the reference's arithmetic). */
+  AMCL_OPT_RESAMPLE_PREFIX = 2,
+  /* Weighting kernel: 0 = automatic, 1 = one thread per particle over the whole
+   * cloud, 2 = two-phase (point tiles across the GPU, then ordered per-particle
+   * sums from a device scratch buffer). */
+  AMCL_OPT_WEIGHT_KERNEL = 3,
+  /* Seed of the counter-based generator (resets its counter). */
+  AMCL_OPT_SEED = 4
+};
+int amcl_pf_set_option(amcl_pf_t pf, int option, int64_t value);
+
+/* Debug/parity: the four normal draws (x, y, z, a order) of the last predict or
+ * init, 4*size floats.  Recorded only while enabled. */
+int amcl_pf_record_draws(amcl_pf_t pf, int enable);
+int amcl_pf_get_draws(amcl_pf_t pf, float* out, uint32_t cap_floats);
+/* Debug/parity: the last resample's source index per output particle. */
+int amcl_pf_get_resample_index(amcl_pf_t pf, int32_t* out, uint32_t cap);
+
+/* Raw stream of the handle (cudaStream_t), for callers that time it with events. */
+int amcl_pf_stream(amcl_pf_t pf, void** stream);
+int amcl_grid_stream(amcl_grid_t g, void** stream);
+
+/* ---- profiling: device time per kernel family, measured with CUDA events ---------- */
+enum
+{
+  AMCL_PROF_CLOUD_WEIGHT = 0, /* the per-particle cloud weighting kernel(s)      */
+  AMCL_PROF_NORMALIZE = 1,    /* blend + normalisation + mean                     */
+  AMCL_PROF_RESAMPLE = 2,
+  AMCL_PROF_PREDICT = 3,
+  AMCL_PROF_DISTANCE_FIELD = 4,
+  AMCL_PROF_COUNT = 5
+};
+/* Enables event pairs around each kernel family on the filter's stream. */
+int amcl_pf_profile(amcl_pf_t pf, int enable);
+/* Synchronises and returns the accumulated milliseconds and launch counts. */
+int amcl_pf_profile_read(amcl_pf_t pf, double ms[AMCL_PROF_COUNT], uint64_t launches[AMCL_PROF_COUNT],
+                         int reset);
+/* Kernel launches issued so far by this process (all handles). */
+uint64_t amcl_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AMCL3D_GPU_H */
