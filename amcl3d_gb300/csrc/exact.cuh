@@ -112,6 +112,38 @@ __device__ __forceinline__ int x320_cmp(const X320& a, const X320& b)
   return 0;
 }
 
+__host__ __device__ inline int clz64(uint64_t x)
+{
+#ifdef __CUDA_ARCH__
+  return __clzll(static_cast<long long>(x));
+#else
+  return x ? __builtin_clzll(x) : 64;
+#endif
+}
+
+// Bits [p, p+64) of a 320-bit magnitude, 0 <= p < 320 (bits past the top are 0).
+__host__ __device__ inline uint64_t x320_bits64(const X320& a, int p)
+{
+  const int w = p >> 6, s = p & 63;
+  const uint64_t lo = w < 5 ? a.w[w] : 0ull;
+  const uint64_t hi = w + 1 < 5 ? a.w[w + 1] : 0ull;
+  return s ? ((lo >> s) | (hi << (64 - s))) : lo;
+}
+
+// True when any bit below position p (exclusive) is set.
+__host__ __device__ inline bool x320_any_below(const X320& a, int p)
+{
+  if (p <= 0)
+    return false;
+  const int w = p >> 6, s = p & 63;
+  for (int i = 0; i < w && i < 5; ++i)
+    if (a.w[i])
+      return true;
+  if (w < 5 && s && (a.w[w] & ((1ull << s) - 1ull)))
+    return true;
+  return false;
+}
+
 // Correctly rounded (nearest, ties to even) conversion to double.
 __host__ __device__ inline double x320_to_double(const X320& v)
 {
@@ -132,31 +164,18 @@ __host__ __device__ inline double x320_to_double(const X320& v)
   for (int i = 4; i >= 0; --i)
     if (a.w[i])
     {
-      int lz = 0;
-      uint64_t x = a.w[i];
-      while (!(x >> 63))
-      {
-        x <<= 1;
-        ++lz;
-      }
-      top = i * 64 + 63 - lz;
+      top = i * 64 + 63 - clz64(a.w[i]);
       break;
     }
   if (top < 0)
     return neg ? -0.0 : 0.0;
-  // bit(i) of the magnitude
-  auto bit = [&](int i) -> uint64_t { return (i < 0) ? 0ull : ((a.w[i >> 6] >> (i & 63)) & 1ull); };
-  uint64_t mant = 0;
   const int lsb = top - 52;  // position of the last kept bit
-  for (int i = top; i >= lsb && i >= 0; --i)
-    mant = (mant << 1) | bit(i);
+  uint64_t mant = lsb >= 0 ? (x320_bits64(a, lsb) & ((1ull << 53) - 1ull)) : x320_bits64(a, 0);
   int exp2 = (lsb >= 0 ? lsb : 0) - 149;  // value = mant * 2^exp2
   if (lsb > 0)
   {
-    const uint64_t guard = bit(lsb - 1);
-    bool sticky = false;
-    for (int i = lsb - 2; i >= 0 && !sticky; --i)
-      sticky = bit(i) != 0;
+    const uint64_t guard = (x320_bits64(a, lsb - 1) & 1ull);
+    const bool sticky = x320_any_below(a, lsb - 1);
     if (guard && (sticky || (mant & 1ull)))
     {
       mant += 1;

@@ -88,7 +88,8 @@ __global__ __launch_bounds__(WT_THREADS) void k_weight_fused(WeightArgs a, GridV
   float4* s_rg = s_pts + WT_CHUNK;
   X320* s_part = reinterpret_cast<X320*>(s_rg + MAX_RANGES);
   float* s_tab = reinterpret_cast<float*>(s_part + 2 * (WT_THREADS / 32));
-  const uint32_t ntab = g.size[0] + g.size[1] + g.size[2] + 3;
+  // The locate tables are only read per point (a range-only update has no grid).
+  const uint32_t ntab = a.N ? g.size[0] + g.size[1] + g.size[2] + 3 : 0u;
   for (uint32_t i = threadIdx.x; i < ntab; i += blockDim.x)
     s_tab[i] = g.T[i];
   for (uint32_t i = threadIdx.x; i < a.nr; i += blockDim.x)
@@ -445,16 +446,21 @@ int launch_cloud_weight(amcl_grid_s* g, const WeightArgs& a, cudaStream_t s)
     return fail(AMCL_ERANGE, "update: more than 64 range measurements");
   if (a.P == 0)
     return AMCL_OK;
-  if (a.kernel == 2 && (!a.scratch || a.scratch_floats < two_phase_scratch_floats(a.P, a.N)))
+  WeightArgs b = a;
+  if (b.N == 0)
+    b.kernel = 1;  // no points: nothing to spread, the fused kernel writes wp = 0
+  if (b.kernel == 2 && (!b.scratch || b.scratch_floats < two_phase_scratch_floats(b.P, b.N)))
     return fail(AMCL_EINVAL, "two-phase weighting without a large enough scratch buffer");
+  if (b.N && !g->view.T)
+    return fail(AMCL_ESTATE, "cloud weighting without a built grid");
   switch (g->view.storage)
   {
     case AMCL_GRID_F16:
-      return launch_storage<AMCL_GRID_F16>(a, g->view, s);
+      return launch_storage<AMCL_GRID_F16>(b, g->view, s);
     case AMCL_GRID_U8:
-      return launch_storage<AMCL_GRID_U8>(a, g->view, s);
+      return launch_storage<AMCL_GRID_U8>(b, g->view, s);
     default:
-      return launch_storage<AMCL_GRID_F32>(a, g->view, s);
+      return launch_storage<AMCL_GRID_F32>(b, g->view, s);
   }
 }
 }  // namespace amcl

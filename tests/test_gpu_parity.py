@@ -59,7 +59,10 @@ def test_distance_field_exact(amcl, ref_small, ref_kat):
 def test_distance_field_fixture_and_slice(amcl, refdata, ref_kat):
     """The reference's map-cloud fixture (179,551 points, 522x384x153 cells): squared
     distances equal the reference's everywhere, and the z = 1.0 slice reproduces
-    nav_msg.bin with the reference's own 33 mismatches."""
+    nav_msg.bin with the reference's own 33 mismatches.  This snapshot's
+    buildGridSliceMsg sizes the slice point2grid(max) - point2grid(min) =
+    522 + 384*522 = 200970 values (the verbatim reference gives the same); the
+    fixture, from an older version, holds the 522x384 layer, i.e. the first 200448."""
     G = amcl.Grid3d()
     G.buildGridMap(refdata["map_points"], (0.0, 0.0, 0.0), (26.1, 19.2, 7.65), 0.05, 0.05)
     d, _ = G.read_cells()
@@ -68,7 +71,9 @@ def test_distance_field_fixture_and_slice(amcl, refdata, ref_kat):
     assert out is not None
     sl, w, h = out
     assert (w, h) == (522, 384)
-    assert int((sl != refdata["nav_slice"]).sum()) == ref_kat["slice_mismatch"]
+    assert sl.size == 522 + 384 * 522
+    nav = refdata["nav_slice"]
+    assert int((sl[: nav.size] != nav).sum()) == ref_kat["slice_mismatch"]
     assert G.buildGridSliceMsg(-100.0) is None  # Grid3dTest.cpp:77-79
     # KAT pose of Grid3dTest.cpp:128-168 on the rebuilt grid (unpinned against 3.8109)
     kat = G.computeCloudWeight(refdata["scan"], 20.017967, 10.140815, 3.372801, 0.0, 0.0, 0.166781)
