@@ -557,6 +557,13 @@ int pf_update_impl(amcl_pf_s* pf, amcl_grid_s* g, const float4* cloud_dev, uint3
     a.kernel = 1;
     gg = &local;
   }
+  else if (!g->built)
+  {
+    // No grid: isIntoMap is false for every particle (Grid3d.cpp:203-204), so no
+    // point is ever weighed; every w becomes 0.
+    a.N = 0;
+    a.kernel = 1;
+  }
   else
     grid_apply_l2_window(g, s);
   if (a.kernel == 2)

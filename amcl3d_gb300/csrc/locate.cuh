@@ -53,6 +53,10 @@ struct PartXf
   float r[9];
   float H[3], L[3];
   double off[3];
+  // All three offsets are exact floats (L == 0).  Then fl64(s + H) is the exact
+  // sum of two floats, or rounds only bits far below the float rounding point, so
+  // X = fl32(fl64(s + H)) equals the single float add s + H: no estimate needed.
+  int exact;
 };
 
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
@@ -91,6 +95,26 @@ __device__ __forceinline__ void make_partxf(const GridView& g, float sr, float c
     p.H[a] = __double2float_rn(off);
     p.L[a] = __double2float_rn(__dsub_rn(off, static_cast<double>(p.H[a])));
   }
+  p.exact = (p.off[0] == static_cast<double>(p.H[0]) && p.off[1] == static_cast<double>(p.H[1]) &&
+             p.off[2] == static_cast<double>(p.H[2]) && isfinite(p.H[0]) && isfinite(p.H[1]) && isfinite(p.H[2]))
+                ? 1
+                : 0;
+}
+
+// Cell index along one axis for an exact X, -1 when the point is rejected
+// (X < 0, X >= V, NaN).  The float estimate floor(X / res) is within one cell of
+// the reference's floor(fl64(X / res)); the table settles it exactly.
+__device__ __forceinline__ int locate_axis_fast(float X, const float* T, float V, float inv_res, int size)
+{
+  if (!(X < V))
+    return -1;
+  int k = __float2int_rd(fmul(X, inv_res));
+  k = min(max(k, 0), size - 1);
+  if (X < T[k])
+    k -= 1;  // X < 0 ends at -1 (T[0] = 0)
+  else if (X >= T[k + 1])
+    k += 1;
+  return k;
 }
 
 // Cell index along one axis for an exact X, -1 when the point is rejected.
@@ -144,6 +168,16 @@ __device__ __forceinline__ int64_t cell_of_point(const GridView& g, const float*
   s[1] = fadd(fadd(fmul(px, p.r[3]), fmul(py, p.r[4])), fmul(pz0, p.r[5]));
   s[2] = fadd(fadd(fmul(px, p.r[6]), fmul(py, p.r[7])), fmul(pz0, p.r[8]));
   int k[3];
+  if (p.exact)
+  {
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+      k[a] = locate_axis_fast(fadd(s[a], p.H[a]), tab + g.toff[a], g.V[a], g.inv_res[a], static_cast<int>(g.size[a]));
+    if ((k[0] | k[1] | k[2]) < 0)
+      return -1;
+    return static_cast<int64_t>(static_cast<uint32_t>(k[0]) + static_cast<uint32_t>(k[1]) * g.step_y +
+                                static_cast<uint32_t>(k[2]) * g.step_z);
+  }
   bool amb = false;
 #pragma unroll
   for (int a = 0; a < 3; ++a)
