@@ -74,6 +74,7 @@ _SIGS = {
     "amcl_grid_set_l2_window": [_vp, _int],
     "amcl_grid_is_into_map": [_vp, _f, _f, _f, C.POINTER(_int)],
     "amcl_grid_cloud_weights": [_vp, _fp, _u32, _fp, _u32, _u32, _f, _f, _fp],
+    "amcl_grid_cloud_weights_noalloc": [_vp, _vp, _u32, _vp, _u32, _f, _f, _vp, _vp],
     "amcl_grid_slice": [_vp, _d, C.POINTER(C.c_int8), _u64, C.POINTER(_u64), C.POINTER(_u32), C.POINTER(_u32)],
     "amcl_grid_stream": [_vp, C.POINTER(_vp)],
     "amcl_pf_create": [C.POINTER(_vp), _u64, _vp],

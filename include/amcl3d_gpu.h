@@ -117,6 +117,20 @@ int amcl_grid_is_into_map(amcl_grid_t g, float x, float y, float z, int* inside)
 int amcl_grid_cloud_weights(amcl_grid_t g, const float* poses4, uint32_t P, const float* xyz, uint32_t n,
                             uint32_t stride_floats, float roll, float pitch, float* out);
 
+/* No counterpart in the reference.  The same weights as amcl_grid_cloud_weights
+ * for callers that must not allocate device memory (a real-time loop that may not
+ * enter the driver's allocator, memory handed out only by a host framework's pool):
+ * nothing is allocated; the two-phase kernel's scratch is a fixed 16 MiB
+ * file-scope device array that every GPU loading the library holds until exit.
+ * poses (P x float4 x, y, z, yaw) and cloud (n x float4 x, y, z, unused) are
+ * 16-byte aligned device buffers, out is P device floats; the call runs on `stream`
+ * (NULL: the default stream) and synchronises it.  Limits: P <= 65536 and
+ * ceil(P/32)*32*n <= 4194304, else AMCL_ERANGE.  All calls share the array, so calls
+ * that overlap on the GPU race.  The first call on a device looks the array's
+ * address up; make it before any stream capture. */
+int amcl_grid_cloud_weights_noalloc(amcl_grid_t g, const void* poses_f4_dev, uint32_t P, const void* cloud_f4_dev,
+                                    uint32_t n, float roll, float pitch, float* out_dev, void* stream);
+
 /* Grid3d::buildGridSliceMsg (Grid3d.cpp:80-121): int8 occupancy of the z slice,
  * prob scaled to 0..100 by the slice maximum.  Writes min(cap, len) values; *len,
  * *width, *height receive the message sizes.  AMCL_EINVAL when z is outside the map. */
