@@ -1,0 +1,1173 @@
+// Many particle filters stepped together: one launch sequence (predict, cloud
+// weights, blend, normalise + mean, resample) for every filter with a staged step,
+// captured once in a CUDA graph and replayed.
+//
+// Memory: fixed arenas sized at creation (the HBM budget new filters are admitted
+// against): particle SoA arrays double-buffered like a single filter's, one range of
+// 256-aligned particles per filter slot; clouds, ranges and the per-step descriptors
+// are packed each step into pinned staging and copied with one transfer each.
+//
+// Work distribution: every kernel runs a fixed grid (a multiple of the SM count) and
+// walks a list of work items, so grid shapes never change with the batch composition
+// and the captured graph stays valid; only the copy sizes are updated per step.  The
+// cloud weighting takes (filter, particle tile) items, longest first, from a global
+// atomic counter (no spin-waits).  Each item is the fused one-thread-per-particle
+// weighting of a single filter, so every filter's weights, sums, mean and resample
+// indices are bit-identical to stepping it alone (the normalisation sums are exact
+// integer sums, independent of how items interleave).
+//
+// Tuning: the particle tile (threads per block of the weighting kernel) and the point
+// tile (scan points staged in shared memory per iteration) are chosen by
+// amcl_batch_autotune, which times the weighting phase of the staged step under each
+// candidate shape.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "filter_dev.cuh"
+#include "grid.cuh"
+#include "weight_dev.cuh"
+
+using namespace amcl;
+
+namespace
+{
+enum : uint32_t
+{
+  ST_PREDICT = 1,
+  ST_UPDATE = 2,
+  ST_RESAMPLE = 4
+};
+
+struct SlotStep
+{
+  uint32_t slot, flags, P, N, nr, cur;
+  uint64_t p_off, c_off;
+  uint32_t r_off, cloud_sum;
+  float sr, cr, sp, cp, k1, k2;
+  int yaw_only;
+  double alpha;
+  PredictArgs pred;
+  float factor, r;
+  GridView g;
+};
+
+struct BatchDev
+{
+  float4* pose[2];
+  float* w[2];
+  float* wp[2];
+  float* wr[2];
+  uint8_t* inmap;
+  int32_t* hi;
+  X320* blocksum;
+  unsigned long long* acc;  // per slot ACC_WORDS
+  PFStats* stats;           // per slot
+  const float4* cloud;
+  const float4* ranges;
+  const SlotStep* steps;
+  const uint32_t* counts;  // [0] steps, [1] block items, [2] weight items
+  const uint2* blk_items;  // (step, local block)
+  const uint2* wt_items;   // (step, particle tile)
+  unsigned int* counter;   // weighting work queue
+};
+
+constexpr int GRID_BLOCKS_PER_SM = 4;
+
+__global__ __launch_bounds__(NT) void k_b_predict(BatchDev d)
+{
+  const uint32_t nitems = d.counts[1];
+  for (uint32_t it = blockIdx.x; it < nitems; it += gridDim.x)
+  {
+    const uint2 bi = d.blk_items[it];
+    const SlotStep& st = d.steps[bi.x];
+    if (!(st.flags & ST_PREDICT))
+      continue;
+    const uint32_t i = bi.y * NT + threadIdx.x;
+    if (i < st.P)
+      predict_particle(i, d.pose[st.cur] + st.p_off, st.pred);
+  }
+}
+
+template <int STORAGE, int SUM>
+__device__ __forceinline__ void b_weigh(const BatchDev& d, const SlotStep& st, uint32_t tile, uint32_t chunk,
+                                        float4* s_pts, const float4* s_rg, X320* s_part, const float2* s_tab)
+{
+  WeightArgs a{};
+  a.pose = d.pose[st.cur] + st.p_off;
+  a.P = st.P;
+  a.cloud = d.cloud + st.c_off;
+  a.N = st.N;
+  a.sr = st.sr;
+  a.cr = st.cr;
+  a.sp = st.sp;
+  a.cp = st.cp;
+  a.nr = st.nr;
+  a.k1 = st.k1;
+  a.k2 = st.k2;
+  a.wp = d.wp[st.cur] + st.p_off;
+  a.wr = d.wr[st.cur] + st.p_off;
+  a.inmap = d.inmap + st.p_off;
+  a.acc_wp = d.acc + static_cast<uint64_t>(st.slot) * ACC_WORDS + ACC_WP * NDIG;
+  a.acc_wr = d.acc + static_cast<uint64_t>(st.slot) * ACC_WORDS + ACC_WR * NDIG;
+  a.yaw_only = st.yaw_only;
+  weigh_block<STORAGE, SUM>(a, st.g, tile * blockDim.x, chunk, s_pts, s_rg, s_part, s_tab);
+}
+
+// Persistent: blocks take (filter, particle tile) items until the queue is empty.
+__global__ void k_b_weight(BatchDev d, uint32_t chunk, uint32_t tab_cap)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  float4* s_pts = reinterpret_cast<float4*>(smem);
+  float4* s_rg = s_pts + chunk;
+  X320* s_part = reinterpret_cast<X320*>(s_rg + MAX_RANGES);
+  float2* s_tab = reinterpret_cast<float2*>(s_part + 2 * 32);
+  __shared__ uint32_t s_item;
+  __shared__ int s_loaded;
+  const uint32_t nitems = d.counts[2];
+  if (threadIdx.x == 0)
+    s_loaded = -1;
+  while (true)
+  {
+    __syncthreads();
+    if (threadIdx.x == 0)
+      s_item = atomicAdd(d.counter, 1u);
+    __syncthreads();
+    const uint32_t it = s_item;
+    if (it >= nitems)
+      break;
+    const uint2 wi = d.wt_items[it];
+    const SlotStep& st = d.steps[wi.x];
+    if (s_loaded != static_cast<int>(wi.x))
+    {
+      if (st.N && table_entries(st.g) <= tab_cap)
+        load_tables(st.g, s_tab);
+      for (uint32_t i = threadIdx.x; i < st.nr; i += blockDim.x)
+        s_rg[i] = d.ranges[st.r_off + i];
+      __syncthreads();
+      if (threadIdx.x == 0)
+        s_loaded = static_cast<int>(wi.x);
+    }
+    const int storage = st.g.storage;
+    if (st.cloud_sum == 0)
+    {
+      if (storage == AMCL_GRID_F16)
+        b_weigh<AMCL_GRID_F16, 0>(d, st, wi.y, chunk, s_pts, s_rg, s_part, s_tab);
+      else if (storage == AMCL_GRID_U8)
+        b_weigh<AMCL_GRID_U8, 0>(d, st, wi.y, chunk, s_pts, s_rg, s_part, s_tab);
+      else
+        b_weigh<AMCL_GRID_F32, 0>(d, st, wi.y, chunk, s_pts, s_rg, s_part, s_tab);
+    }
+    else
+    {
+      if (storage == AMCL_GRID_F16)
+        b_weigh<AMCL_GRID_F16, 1>(d, st, wi.y, chunk, s_pts, s_rg, s_part, s_tab);
+      else if (storage == AMCL_GRID_U8)
+        b_weigh<AMCL_GRID_U8, 1>(d, st, wi.y, chunk, s_pts, s_rg, s_part, s_tab);
+      else
+        b_weigh<AMCL_GRID_F32, 1>(d, st, wi.y, chunk, s_pts, s_rg, s_part, s_tab);
+    }
+  }
+}
+
+__global__ __launch_bounds__(NT) void k_b_blend(BatchDev d)
+{
+  __shared__ double s_sum[2];
+  __shared__ X320 s_part[NT / 32];
+  const uint32_t nitems = d.counts[1];
+  for (uint32_t it = blockIdx.x; it < nitems; it += gridDim.x)
+  {
+    const uint2 bi = d.blk_items[it];
+    const SlotStep& st = d.steps[bi.x];
+    if (!(st.flags & ST_UPDATE))
+      continue;
+    blend_block(bi.y, st.P, d.inmap + st.p_off, d.wp[st.cur] + st.p_off, d.wr[st.cur] + st.p_off,
+                d.w[st.cur] + st.p_off, st.alpha, d.acc + static_cast<uint64_t>(st.slot) * ACC_WORDS, s_sum, s_part);
+  }
+}
+
+__global__ __launch_bounds__(NT) void k_b_normalize(BatchDev d)
+{
+  __shared__ double s_sum[2];
+  __shared__ X320 s_part[NT / 32];
+  const uint32_t nitems = d.counts[1];
+  for (uint32_t it = blockIdx.x; it < nitems; it += gridDim.x)
+  {
+    const uint2 bi = d.blk_items[it];
+    const SlotStep& st = d.steps[bi.x];
+    if (!(st.flags & ST_UPDATE))
+      continue;
+    normalize_block(bi.y, st.P, d.pose[st.cur] + st.p_off, d.w[st.cur] + st.p_off,
+                    d.acc + static_cast<uint64_t>(st.slot) * ACC_WORDS, d.blocksum + st.p_off / NT, s_sum, s_part);
+  }
+}
+
+__global__ void k_b_finalize(BatchDev d)
+{
+  const uint32_t n = d.counts[0];
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
+  {
+    const SlotStep& st = d.steps[s];
+    if (st.flags & ST_UPDATE)
+      finalize_stats(d.acc + static_cast<uint64_t>(st.slot) * ACC_WORDS, d.stats + st.slot);
+  }
+}
+
+__global__ __launch_bounds__(NT) void k_b_prefix(BatchDev d)
+{
+  __shared__ X320 s_scan[NT / 32];
+  __shared__ X320 s_base;
+  const uint32_t nitems = d.counts[1];
+  for (uint32_t it = blockIdx.x; it < nitems; it += gridDim.x)
+  {
+    const uint2 bi = d.blk_items[it];
+    const SlotStep& st = d.steps[bi.x];
+    if (!(st.flags & ST_RESAMPLE))
+      continue;
+    prefix_hi_block(bi.y, st.P, d.w[st.cur] + st.p_off, d.blocksum + st.p_off / NT, st.r, st.factor,
+                    d.hi + st.p_off, s_scan, &s_base);
+  }
+}
+
+__global__ __launch_bounds__(NT) void k_b_gather(BatchDev d)
+{
+  const uint32_t nitems = d.counts[1];
+  for (uint32_t it = blockIdx.x; it < nitems; it += gridDim.x)
+  {
+    const uint2 bi = d.blk_items[it];
+    const SlotStep& st = d.steps[bi.x];
+    if (!(st.flags & ST_RESAMPLE))
+      continue;
+    const uint32_t m = bi.y * NT + threadIdx.x;
+    if (m < st.P)
+    {
+      const uint32_t o = 1 - st.cur;
+      gather_particle(m, st.P, d.hi + st.p_off, d.pose[st.cur] + st.p_off, d.wp[st.cur] + st.p_off,
+                      d.wr[st.cur] + st.p_off, d.pose[o] + st.p_off, d.w[o] + st.p_off, d.wp[o] + st.p_off,
+                      d.wr[o] + st.p_off, st.factor, nullptr);
+    }
+  }
+}
+}  // namespace
+
+// ---- host side ------------------------------------------------------------------------------------
+
+struct BatchSlot
+{
+  bool used = false;
+  amcl_grid_s* grid = nullptr;
+  uint32_t cap = 0;
+  uint64_t p_off = 0;
+  uint32_t P = 0;
+  uint64_t seed = 0, step = 0;
+  int cur = 0;
+  bool initialized = false;
+  int cloud_sum = 0;
+  // staged step
+  bool staged = false;
+  std::vector<float4> cloud;
+  std::vector<float4> ranges;
+  bool predict = false;
+  double odom[8] = {};
+  double alpha = 0.5, sigma = 0.1, roll = 0, pitch = 0;
+  bool resample = false;
+  bool stats_valid = false;
+};
+
+struct amcl_batch_s
+{
+  StreamHolder st;
+  uint32_t max_filters = 0;
+  uint64_t max_particles = 0, max_points = 0;
+  std::vector<BatchSlot> slots;
+  std::vector<std::pair<uint64_t, uint64_t>> free_ranges;  // particle arena [off, len)
+  DevBuf pose[2], w[2], wp[2], wr[2], inmap, hi, blocksum, acc, stats, cloud, ranges, steps, counts, blk_items,
+      wt_items, counter;
+  PinnedBuf h_cloud, h_ranges, h_steps, h_counts, h_blk, h_wt, h_stats;
+  uint32_t n_steps = 0, n_blk = 0, n_wt = 0;
+  uint64_t n_cloud = 0, n_ranges = 0;
+  std::vector<uint32_t> step_slots;  // slot of each step in the last launch
+  int threads = 256, chunk = 1024;
+  uint32_t tab_cap = 0;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph = nullptr;
+  int graph_threads = 0, graph_chunk = 0;
+  cudaGraphNode_t n_cloud_cp = nullptr, n_ranges_cp = nullptr, n_steps_cp = nullptr, n_counts_cp = nullptr,
+                  n_blk_cp = nullptr, n_wt_cp = nullptr, n_stats_cp = nullptr;
+  bool in_flight = false;
+  uint64_t steps_done = 0;
+  std::mutex mu;
+  ~amcl_batch_s()
+  {
+    if (exec)
+      cudaGraphExecDestroy(exec);
+    if (graph)
+      cudaGraphDestroy(graph);
+  }
+};
+
+namespace
+{
+uint64_t align256(uint64_t v) { return (v + 255) & ~255ull; }
+
+BatchDev batch_dev(amcl_batch_s* b)
+{
+  BatchDev d;
+  for (int k = 0; k < 2; ++k)
+  {
+    d.pose[k] = b->pose[k].as<float4>();
+    d.w[k] = b->w[k].as<float>();
+    d.wp[k] = b->wp[k].as<float>();
+    d.wr[k] = b->wr[k].as<float>();
+  }
+  d.inmap = b->inmap.as<uint8_t>();
+  d.hi = b->hi.as<int32_t>();
+  d.blocksum = b->blocksum.as<X320>();
+  d.acc = b->acc.as<unsigned long long>();
+  d.stats = b->stats.as<PFStats>();
+  d.cloud = b->cloud.as<float4>();
+  d.ranges = b->ranges.as<float4>();
+  d.steps = b->steps.as<SlotStep>();
+  d.counts = b->counts.as<uint32_t>();
+  d.blk_items = b->blk_items.as<uint2>();
+  d.wt_items = b->wt_items.as<uint2>();
+  d.counter = b->counter.as<unsigned int>();
+  return d;
+}
+
+size_t weight_smem(const amcl_batch_s* b, int chunk)
+{
+  return static_cast<size_t>(chunk) * sizeof(float4) + MAX_RANGES * sizeof(float4) + 64 * sizeof(X320) +
+         static_cast<size_t>(b->tab_cap) * sizeof(float2);
+}
+
+// Enqueues the whole step on the batch stream (also what the graph captures).
+int enqueue_step(amcl_batch_s* b, int threads, int chunk, bool copies)
+{
+  cudaStream_t s = b->st.s;
+  BatchDev d = batch_dev(b);
+  const int sms = device_sm_count();
+  const unsigned grid = static_cast<unsigned>(sms * GRID_BLOCKS_PER_SM);
+  if (copies)
+  {
+    AMCL_CUDA_TRY(cudaMemcpyAsync(b->counts.p, b->h_counts.p, 4 * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    AMCL_CUDA_TRY(cudaMemcpyAsync(b->steps.p, b->h_steps.p, std::max<uint64_t>(b->n_steps, 1) * sizeof(SlotStep),
+                                  cudaMemcpyHostToDevice, s));
+    AMCL_CUDA_TRY(cudaMemcpyAsync(b->blk_items.p, b->h_blk.p, std::max<uint64_t>(b->n_blk, 1) * sizeof(uint2),
+                                  cudaMemcpyHostToDevice, s));
+    AMCL_CUDA_TRY(cudaMemcpyAsync(b->wt_items.p, b->h_wt.p, std::max<uint64_t>(b->n_wt, 1) * sizeof(uint2),
+                                  cudaMemcpyHostToDevice, s));
+    AMCL_CUDA_TRY(cudaMemcpyAsync(b->cloud.p, b->h_cloud.p, std::max<uint64_t>(b->n_cloud, 1) * sizeof(float4),
+                                  cudaMemcpyHostToDevice, s));
+    AMCL_CUDA_TRY(cudaMemcpyAsync(b->ranges.p, b->h_ranges.p, std::max<uint64_t>(b->n_ranges, 1) * sizeof(float4),
+                                  cudaMemcpyHostToDevice, s));
+  }
+  k_b_predict<<<grid, NT, 0, s>>>(d);
+  AMCL_LAUNCH_CHECK("k_b_predict");
+  AMCL_CUDA_TRY(cudaMemsetAsync(b->acc.p, 0, static_cast<size_t>(b->max_filters) * ACC_WORDS * 8, s));
+  AMCL_CUDA_TRY(cudaMemsetAsync(b->counter.p, 0, sizeof(unsigned int), s));
+  k_b_weight<<<static_cast<unsigned>(sms * 2), threads, weight_smem(b, chunk), s>>>(d, static_cast<uint32_t>(chunk),
+                                                                                   b->tab_cap);
+  AMCL_LAUNCH_CHECK("k_b_weight");
+  k_b_blend<<<grid, NT, 0, s>>>(d);
+  AMCL_LAUNCH_CHECK("k_b_blend");
+  k_b_normalize<<<grid, NT, 0, s>>>(d);
+  AMCL_LAUNCH_CHECK("k_b_normalize");
+  k_b_finalize<<<1, 256, 0, s>>>(d);
+  AMCL_LAUNCH_CHECK("k_b_finalize");
+  k_b_prefix<<<grid, NT, 0, s>>>(d);
+  AMCL_LAUNCH_CHECK("k_b_prefix");
+  k_b_gather<<<grid, NT, 0, s>>>(d);
+  AMCL_LAUNCH_CHECK("k_b_gather");
+  if (copies)
+    AMCL_CUDA_TRY(cudaMemcpyAsync(b->h_stats.p, b->stats.p, static_cast<size_t>(b->max_filters) * sizeof(PFStats),
+                                  cudaMemcpyDeviceToHost, s));
+  return AMCL_OK;
+}
+
+// Packs the staged steps of every slot into the pinned staging buffers.
+int pack_steps(amcl_batch_s* b)
+{
+  SlotStep* hs = b->h_steps.as<SlotStep>();
+  uint2* hb = b->h_blk.as<uint2>();
+  uint2* hw = b->h_wt.as<uint2>();
+  float4* hc = b->h_cloud.as<float4>();
+  float4* hr = b->h_ranges.as<float4>();
+  uint32_t ns = 0, nb = 0;
+  uint64_t nc = 0, nr = 0;
+  std::vector<std::pair<uint64_t, uint2>> wt;  // (cost, item)
+  b->step_slots.clear();
+  const int threads = b->threads;
+  for (uint32_t si = 0; si < b->slots.size(); ++si)
+  {
+    BatchSlot& sl = b->slots[si];
+    if (!sl.used || !sl.staged)
+      continue;
+    if (!sl.P)
+    {
+      sl.staged = false;
+      continue;
+    }
+    SlotStep st{};
+    st.slot = si;
+    st.P = sl.P;
+    st.cur = static_cast<uint32_t>(sl.cur);
+    st.p_off = sl.p_off;
+    const bool upd = sl.grid && sl.grid->built;
+    st.N = upd ? static_cast<uint32_t>(sl.cloud.size()) : 0;
+    st.nr = static_cast<uint32_t>(sl.ranges.size());
+    if (nc + st.N > b->max_points)
+      return fail(AMCL_ERANGE, "batch: staged clouds exceed max_points_per_step");
+    st.c_off = nc;
+    if (st.N)
+      std::memcpy(hc + nc, sl.cloud.data(), st.N * sizeof(float4));
+    nc += st.N;
+    st.r_off = static_cast<uint32_t>(nr);
+    if (st.nr)
+      std::memcpy(hr + nr, sl.ranges.data(), st.nr * sizeof(float4));
+    nr += st.nr;
+    st.flags = ST_UPDATE | (sl.predict ? ST_PREDICT : 0u) | (sl.resample ? ST_RESAMPLE : 0u);
+    st.cloud_sum = static_cast<uint32_t>(sl.cloud_sum);
+    const float rollf = static_cast<float>(sl.roll), pitchf = static_cast<float>(sl.pitch);
+    st.sr = sinf(rollf);
+    st.cr = cosf(rollf);
+    st.sp = sinf(pitchf);
+    st.cp = cosf(pitchf);
+    st.yaw_only = (st.sr == 0.0f && st.sp == 0.0f && st.cr == 1.0f && st.cp == 1.0f) ? 1 : 0;
+    st.k1 = static_cast<float>(1.f / (sl.sigma * std::sqrt(2 * M_PI)));
+    st.k2 = static_cast<float>(0.5f / (sl.sigma * sl.sigma));
+    st.alpha = sl.alpha;
+    if (upd)
+      st.g = sl.grid->view;
+    else
+    {
+      st.g = GridView{};  // no grid: every particle is outside the map
+    }
+    if (sl.predict)
+    {
+      st.pred.n = sl.P;
+      st.pred.seed_lo = static_cast<uint32_t>(sl.seed);
+      st.pred.seed_hi = static_cast<uint32_t>(sl.seed >> 32);
+      st.pred.step = sl.step++;
+      st.pred.sx = static_cast<float>(std::fabs(sl.odom[4] * sl.odom[0]));
+      st.pred.sy = static_cast<float>(std::fabs(sl.odom[5] * sl.odom[1]));
+      st.pred.sz = static_cast<float>(std::fabs(sl.odom[6] * sl.odom[2]));
+      st.pred.sa = static_cast<float>(std::fabs(sl.odom[7] * sl.odom[3]));
+      st.pred.dx = sl.odom[4];
+      st.pred.dy = sl.odom[5];
+      st.pred.dz = sl.odom[6];
+      st.pred.da = sl.odom[7];
+      st.pred.draws = nullptr;
+    }
+    if (sl.resample)
+    {
+      Philox4 c;
+      c.v[0] = 0;
+      c.v[1] = static_cast<uint32_t>(sl.step);
+      c.v[2] = static_cast<uint32_t>(sl.step >> 32);
+      c.v[3] = RNG_TAG_RESAMPLE;
+      const Philox4 r = philox4x32_10(c, static_cast<uint32_t>(sl.seed), static_cast<uint32_t>(sl.seed >> 32));
+      sl.step += 1;
+      const float u = u01_closed0(r.v[0]);
+      st.factor = 1.f / static_cast<float>(sl.P);
+      st.r = st.factor * u;
+    }
+    const uint32_t nblk = ceil_div(sl.P, NT);
+    for (uint32_t k = 0; k < nblk; ++k)
+      hb[nb++] = make_uint2(ns, k);
+    const uint32_t ntile = ceil_div(sl.P, threads);
+    for (uint32_t k = 0; k < ntile; ++k)
+      wt.push_back({ static_cast<uint64_t>(std::max<uint32_t>(st.N, 1)), make_uint2(ns, k) });
+    hs[ns++] = st;
+    b->step_slots.push_back(si);
+    sl.staged = false;
+  }
+  // longest items first (stable: items of one filter stay together for table reuse)
+  std::stable_sort(wt.begin(), wt.end(), [](const std::pair<uint64_t, uint2>& x, const std::pair<uint64_t, uint2>& y) {
+    return x.first > y.first;
+  });
+  for (size_t k = 0; k < wt.size(); ++k)
+    hw[k] = wt[k].second;
+  b->n_steps = ns;
+  b->n_blk = nb;
+  b->n_wt = static_cast<uint32_t>(wt.size());
+  b->n_cloud = nc;
+  b->n_ranges = nr;
+  uint32_t* hcnt = b->h_counts.as<uint32_t>();
+  hcnt[0] = ns;
+  hcnt[1] = nb;
+  hcnt[2] = b->n_wt;
+  hcnt[3] = 0;
+  return AMCL_OK;
+}
+
+int graph_update_copies(amcl_batch_s* b)
+{
+  // The copies in the graph move the full staging capacity only up to what is used.
+  cudaStream_t s = b->st.s;
+  (void)s;
+  struct Cp
+  {
+    cudaGraphNode_t node;
+    void* dst;
+    const void* src;
+    size_t bytes;
+  };
+  const Cp cps[] = {
+    { b->n_steps_cp, b->steps.p, b->h_steps.p, std::max<uint64_t>(b->n_steps, 1) * sizeof(SlotStep) },
+    { b->n_blk_cp, b->blk_items.p, b->h_blk.p, std::max<uint64_t>(b->n_blk, 1) * sizeof(uint2) },
+    { b->n_wt_cp, b->wt_items.p, b->h_wt.p, std::max<uint64_t>(b->n_wt, 1) * sizeof(uint2) },
+    { b->n_cloud_cp, b->cloud.p, b->h_cloud.p, std::max<uint64_t>(b->n_cloud, 1) * sizeof(float4) },
+    { b->n_ranges_cp, b->ranges.p, b->h_ranges.p, std::max<uint64_t>(b->n_ranges, 1) * sizeof(float4) },
+  };
+  for (const Cp& c : cps)
+    AMCL_CUDA_TRY(cudaGraphExecMemcpyNodeSetParams1D(b->exec, c.node, c.dst, c.src, c.bytes, cudaMemcpyHostToDevice));
+  return AMCL_OK;
+}
+
+int build_graph(amcl_batch_s* b)
+{
+  if (b->exec)
+  {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  if (b->graph)
+  {
+    cudaGraphDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  cudaStream_t s = b->st.s;
+  AMCL_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  int rc = enqueue_step(b, b->threads, b->chunk, true);
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(s, &g);
+  if (rc)
+  {
+    if (g)
+      cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess)
+    return fail(AMCL_ECUDA, std::string("batch graph capture: ") + cudaGetErrorString(e));
+  b->graph = g;
+  // Find the memcpy nodes by their destinations.
+  size_t nn = 0;
+  AMCL_CUDA_TRY(cudaGraphGetNodes(g, nullptr, &nn));
+  std::vector<cudaGraphNode_t> nodes(nn);
+  AMCL_CUDA_TRY(cudaGraphGetNodes(g, nodes.data(), &nn));
+  for (cudaGraphNode_t n : nodes)
+  {
+    cudaGraphNodeType t;
+    AMCL_CUDA_TRY(cudaGraphNodeGetType(n, &t));
+    if (t != cudaGraphNodeTypeMemcpy)
+      continue;
+    cudaMemcpy3DParms p;
+    AMCL_CUDA_TRY(cudaGraphMemcpyNodeGetParams(n, &p));
+    const void* dst = p.dstPtr.ptr;
+    if (dst == b->steps.p)
+      b->n_steps_cp = n;
+    else if (dst == b->blk_items.p)
+      b->n_blk_cp = n;
+    else if (dst == b->wt_items.p)
+      b->n_wt_cp = n;
+    else if (dst == b->cloud.p)
+      b->n_cloud_cp = n;
+    else if (dst == b->ranges.p)
+      b->n_ranges_cp = n;
+  }
+  if (!b->n_steps_cp || !b->n_blk_cp || !b->n_wt_cp || !b->n_cloud_cp || !b->n_ranges_cp)
+    return fail(AMCL_ECUDA, "batch graph: copy nodes not found");
+  AMCL_CUDA_TRY(cudaGraphInstantiate(&b->exec, g, 0));
+  b->graph_threads = b->threads;
+  b->graph_chunk = b->chunk;
+  return AMCL_OK;
+}
+
+int batch_wait(amcl_batch_s* b)
+{
+  if (!b->in_flight)
+    return AMCL_OK;
+  AMCL_CUDA_TRY(cudaStreamSynchronize(b->st.s));
+  b->in_flight = false;
+  for (uint32_t si : b->step_slots)
+  {
+    b->slots[si].stats_valid = true;
+  }
+  return AMCL_OK;
+}
+
+int slot_check(amcl_batch_s* b, int slot)
+{
+  if (slot < 0 || static_cast<uint32_t>(slot) >= b->slots.size() || !b->slots[slot].used)
+    return fail(AMCL_EINVAL, "batch: no such filter slot");
+  return AMCL_OK;
+}
+
+// Single-slot helper kernels (init, set/get) reuse the filter bodies directly.
+__global__ __launch_bounds__(NT) void k_slot_init(float4* pose, float* w, float* wp, float* wr, uint32_t n, float x,
+                                                 float y, float z, float a, float xd, float yd, float zd, float ad,
+                                                 float gc1, float gc2, uint32_t seed_lo, uint32_t seed_hi,
+                                                 uint64_t step, unsigned long long* acc)
+{
+  __shared__ X320 s_part[NT / 32];
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  float wv = 0.0f;
+  if (i < n)
+  {
+    float4 p = make_float4(x, y, z, a);
+    wv = gc1;
+    if (i > 0)
+    {
+      Philox4 c;
+      c.v[0] = i;
+      c.v[1] = static_cast<uint32_t>(step);
+      c.v[2] = static_cast<uint32_t>(step >> 32);
+      c.v[3] = RNG_TAG_INIT;
+      float zz[4];
+      normals4(philox4x32_10(c, seed_lo, seed_hi), zz);
+      p.x = fadd(x, fadd(fmul(zz[0], xd), 0.0f));
+      p.y = fadd(y, fadd(fmul(zz[1], yd), 0.0f));
+      p.z = fadd(z, fadd(fmul(zz[2], zd), 0.0f));
+      p.w = fadd(a, fadd(fmul(zz[3], ad), 0.0f));
+      const float dx = fsub(p.x, x), dy = fsub(p.y, y), dz = fsub(p.z, z);
+      const float dist = __fsqrt_rn(fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz)));
+      wv = fmul(gc1, __double2float_rn(exp(static_cast<double>(fmul(fmul(-dist, dist), gc2)))));
+    }
+    pose[i] = p;
+    w[i] = wv;
+    wp[i] = 0.0f;
+    wr[i] = 0.0f;
+  }
+  block_exact_add(x320_from_float(wv), acc + ACC_W * NDIG, s_part);
+}
+
+__global__ __launch_bounds__(NT) void k_slot_normalize(uint32_t n, const float4* pose, float* w,
+                                                      unsigned long long* acc, X320* blocksum)
+{
+  __shared__ double s_sum[2];
+  __shared__ X320 s_part[NT / 32];
+  normalize_block(blockIdx.x, n, pose, w, acc, blocksum, s_sum, s_part);
+}
+
+__global__ void k_slot_finalize(const unsigned long long* acc, PFStats* st)
+{
+  if (threadIdx.x == 0 && blockIdx.x == 0)
+    finalize_stats(acc, st);
+}
+}  // namespace
+
+extern "C" int amcl_batch_create(amcl_batch_t* out, uint32_t max_filters, uint64_t max_particles,
+                                 uint64_t max_points_per_step, void* stream)
+{
+  if (!out || !max_filters || !max_particles || max_filters > (1u << 20) || max_particles > (1ull << 31))
+    return fail(AMCL_EINVAL, "amcl_batch_create: bad arguments");
+  amcl_batch_s* b = new amcl_batch_s();
+  int rc = b->st.init(stream);
+  const uint64_t cap = align256(max_particles) + 256ull * max_filters;  // per-slot alignment slack
+  const uint64_t pts = std::max<uint64_t>(max_points_per_step, 1);
+  const uint64_t rng = 64ull * max_filters;
+  const uint64_t items = cap / 64 + max_filters;  // weight tiles of >= 64 particles
+  for (int k = 0; k < 2 && !rc; ++k)
+    if ((rc = b->pose[k].ensure(cap * 16)) || (rc = b->w[k].ensure(cap * 4)) || (rc = b->wp[k].ensure(cap * 4)) ||
+        (rc = b->wr[k].ensure(cap * 4)))
+      break;
+  if (!rc)
+    (rc = b->inmap.ensure(cap)) || (rc = b->hi.ensure(cap * 4)) || (rc = b->blocksum.ensure(cap / NT * sizeof(X320))) ||
+        (rc = b->acc.ensure(static_cast<size_t>(max_filters) * ACC_WORDS * 8)) ||
+        (rc = b->stats.ensure(static_cast<size_t>(max_filters) * sizeof(PFStats))) ||
+        (rc = b->cloud.ensure(pts * 16)) || (rc = b->ranges.ensure(rng * 16)) ||
+        (rc = b->steps.ensure(static_cast<size_t>(max_filters) * sizeof(SlotStep))) ||
+        (rc = b->counts.ensure(16)) || (rc = b->blk_items.ensure((cap / NT + max_filters) * sizeof(uint2))) ||
+        (rc = b->wt_items.ensure(items * sizeof(uint2))) || (rc = b->counter.ensure(16)) ||
+        (rc = b->h_cloud.ensure(pts * 16)) || (rc = b->h_ranges.ensure(rng * 16)) ||
+        (rc = b->h_steps.ensure(static_cast<size_t>(max_filters) * sizeof(SlotStep))) ||
+        (rc = b->h_counts.ensure(16)) || (rc = b->h_blk.ensure((cap / NT + max_filters) * sizeof(uint2))) ||
+        (rc = b->h_wt.ensure(items * sizeof(uint2))) ||
+        (rc = b->h_stats.ensure(static_cast<size_t>(max_filters) * sizeof(PFStats)));
+  if (!rc && cudaMemsetAsync(b->stats.p, 0, static_cast<size_t>(max_filters) * sizeof(PFStats), b->st.s) != cudaSuccess)
+    rc = fail(AMCL_ECUDA, "amcl_batch_create: memset");
+  if (rc)
+  {
+    delete b;
+    return rc;
+  }
+  std::memset(b->h_stats.p, 0, static_cast<size_t>(max_filters) * sizeof(PFStats));
+  b->max_filters = max_filters;
+  b->max_particles = cap;
+  b->max_points = pts;
+  b->slots.resize(max_filters);
+  b->free_ranges.push_back({ 0, cap });
+  *out = b;
+  return AMCL_OK;
+}
+
+extern "C" int amcl_batch_destroy(amcl_batch_t b)
+{
+  if (!b)
+    return AMCL_OK;
+  cudaStreamSynchronize(b->st.s);
+  delete b;
+  return AMCL_OK;
+}
+
+extern "C" int amcl_batch_add(amcl_batch_t b, amcl_grid_t grid, uint32_t capacity, uint64_t seed, int* slot)
+{
+  if (!b || !slot || !capacity)
+    return fail(AMCL_EINVAL, "amcl_batch_add: bad arguments");
+  std::lock_guard<std::mutex> lock(b->mu);
+  int free_slot = -1;
+  for (uint32_t i = 0; i < b->slots.size(); ++i)
+    if (!b->slots[i].used)
+    {
+      free_slot = static_cast<int>(i);
+      break;
+    }
+  if (free_slot < 0)
+    return fail(AMCL_ENOMEM, "amcl_batch_add: all filter slots are in use");
+  const uint64_t need = align256(capacity);
+  for (size_t k = 0; k < b->free_ranges.size(); ++k)
+  {
+    auto& fr = b->free_ranges[k];
+    if (fr.second >= need)
+    {
+      BatchSlot& sl = b->slots[free_slot];
+      sl = BatchSlot();
+      sl.used = true;
+      sl.grid = grid;
+      sl.cap = static_cast<uint32_t>(need);
+      sl.p_off = fr.first;
+      sl.seed = seed;
+      fr.first += need;
+      fr.second -= need;
+      if (!fr.second)
+        b->free_ranges.erase(b->free_ranges.begin() + static_cast<long>(k));
+      *slot = free_slot;
+      return AMCL_OK;
+    }
+  }
+  return fail(AMCL_ENOMEM, "amcl_batch_add: no particle arena range left (HBM budget)");
+}
+
+extern "C" int amcl_batch_remove(amcl_batch_t b, int slot)
+{
+  if (!b)
+    return fail(AMCL_EINVAL, "amcl_batch_remove: null batch");
+  std::lock_guard<std::mutex> lock(b->mu);
+  int rc = slot_check(b, slot);
+  if (rc)
+    return rc;
+  if ((rc = batch_wait(b)))
+    return rc;
+  BatchSlot& sl = b->slots[slot];
+  b->free_ranges.push_back({ sl.p_off, sl.cap });
+  std::sort(b->free_ranges.begin(), b->free_ranges.end());
+  // coalesce neighbours
+  std::vector<std::pair<uint64_t, uint64_t>> merged;
+  for (auto& fr : b->free_ranges)
+  {
+    if (!merged.empty() && merged.back().first + merged.back().second == fr.first)
+      merged.back().second += fr.second;
+    else
+      merged.push_back(fr);
+  }
+  b->free_ranges.swap(merged);
+  sl = BatchSlot();
+  return AMCL_OK;
+}
+
+extern "C" int amcl_batch_set_grid(amcl_batch_t b, int slot, amcl_grid_t grid)
+{
+  if (!b)
+    return fail(AMCL_EINVAL, "amcl_batch_set_grid: null batch");
+  std::lock_guard<std::mutex> lock(b->mu);
+  int rc = slot_check(b, slot);
+  if (rc)
+    return rc;
+  b->slots[slot].grid = grid;
+  return AMCL_OK;
+}
+
+extern "C" int amcl_batch_init(amcl_batch_t b, int slot, int num_particles, float x, float y, float z, float a,
+                               float x_dev, float y_dev, float z_dev, float a_dev)
+{
+  if (!b)
+    return fail(AMCL_EINVAL, "amcl_batch_init: null batch");
+  std::lock_guard<std::mutex> lock(b->mu);
+  int rc = slot_check(b, slot);
+  if (rc || (rc = batch_wait(b)))
+    return rc;
+  BatchSlot& sl = b->slots[slot];
+  const long long np = num_particles < 0 ? -static_cast<long long>(num_particles) : num_particles;
+  if (np == 0 || static_cast<uint64_t>(np) > sl.cap)
+    return fail(AMCL_ERANGE, "amcl_batch_init: particle count is 0 or above the slot's capacity");
+  sl.P = static_cast<uint32_t>(np);
+  sl.cur = 0;
+  const float dev = std::max(std::max(x_dev, y_dev), z_dev);
+  const float gc1 = static_cast<float>(1. / (dev * std::sqrt(2 * M_PI)));
+  const float two_dev_dev = (2 * dev) * dev;
+  const float gc2 = static_cast<float>(1. / two_dev_dev);
+  cudaStream_t s = b->st.s;
+  unsigned long long* acc = b->acc.as<unsigned long long>() + static_cast<uint64_t>(slot) * ACC_WORDS;
+  AMCL_CUDA_TRY(cudaMemsetAsync(acc, 0, ACC_WORDS * 8, s));
+  const uint64_t off = sl.p_off;
+  k_slot_init<<<ceil_div(sl.P, NT), NT, 0, s>>>(b->pose[0].as<float4>() + off, b->w[0].as<float>() + off,
+                                                b->wp[0].as<float>() + off, b->wr[0].as<float>() + off, sl.P, x, y, z,
+                                                a, x_dev, y_dev, z_dev, a_dev, gc1, gc2, static_cast<uint32_t>(sl.seed),
+                                                static_cast<uint32_t>(sl.seed >> 32), sl.step++, acc);
+  AMCL_LAUNCH_CHECK("k_slot_init");
+  k_slot_normalize<<<ceil_div(sl.P, NT), NT, 0, s>>>(sl.P, b->pose[0].as<float4>() + off, b->w[0].as<float>() + off,
+                                                     acc, b->blocksum.as<X320>() + off / NT);
+  AMCL_LAUNCH_CHECK("k_slot_normalize");
+  k_slot_finalize<<<1, 32, 0, s>>>(acc, b->stats.as<PFStats>() + slot);
+  AMCL_LAUNCH_CHECK("k_slot_finalize");
+  AMCL_CUDA_TRY(cudaMemcpyAsync(b->h_stats.as<PFStats>() + slot, b->stats.as<PFStats>() + slot, sizeof(PFStats),
+                                cudaMemcpyDeviceToHost, s));
+  AMCL_CUDA_TRY(cudaStreamSynchronize(s));
+  sl.initialized = true;
+  sl.stats_valid = true;
+  return AMCL_OK;
+}
+
+extern "C" int amcl_batch_set_particles(amcl_batch_t b, int slot, const float* p7, uint32_t n)
+{
+  if (!b || !p7 || !n)
+    return fail(AMCL_EINVAL, "amcl_batch_set_particles: bad arguments");
+  std::lock_guard<std::mutex> lock(b->mu);
+  int rc = slot_check(b, slot);
+  if (rc || (rc = batch_wait(b)))
+    return rc;
+  BatchSlot& sl = b->slots[slot];
+  if (n > sl.cap)
+    return fail(AMCL_ERANGE, "amcl_batch_set_particles: above the slot's capacity");
+  std::vector<float4> pose(n);
+  std::vector<float> w(n), wp(n), wr(n);
+  for (uint32_t i = 0; i < n; ++i)
+  {
+    const float* q = p7 + 7ull * i;
+    pose[i] = make_float4(q[0], q[1], q[2], q[3]);
+    w[i] = q[4];
+    wp[i] = q[5];
+    wr[i] = q[6];
+  }
+  cudaStream_t s = b->st.s;
+  const uint64_t off = sl.p_off;
+  AMCL_CUDA_TRY(cudaMemcpyAsync(b->pose[0].as<float4>() + off, pose.data(), n * 16ull, cudaMemcpyHostToDevice, s));
+  AMCL_CUDA_TRY(cudaMemcpyAsync(b->w[0].as<float>() + off, w.data(), n * 4ull, cudaMemcpyHostToDevice, s));
+  AMCL_CUDA_TRY(cudaMemcpyAsync(b->wp[0].as<float>() + off, wp.data(), n * 4ull, cudaMemcpyHostToDevice, s));
+  AMCL_CUDA_TRY(cudaMemcpyAsync(b->wr[0].as<float>() + off, wr.data(), n * 4ull, cudaMemcpyHostToDevice, s));
+  AMCL_CUDA_TRY(cudaStreamSynchronize(s));
+  sl.P = n;
+  sl.cur = 0;
+  sl.initialized = true;
+  return AMCL_OK;
+}
+
+extern "C" int amcl_batch_get_particles(amcl_batch_t b, int slot, float* p7, uint32_t cap)
+{
+  if (!b || (!p7 && cap))
+    return fail(AMCL_EINVAL, "amcl_batch_get_particles: bad arguments");
+  std::lock_guard<std::mutex> lock(b->mu);
+  int rc = slot_check(b, slot);
+  if (rc || (rc = batch_wait(b)))
+    return rc;
+  BatchSlot& sl = b->slots[slot];
+  const uint32_t m = std::min(cap, sl.P);
+  if (!m)
+    return AMCL_OK;
+  std::vector<float4> pose(m);
+  std::vector<float> w(m), wp(m), wr(m);
+  cudaStream_t s = b->st.s;
+  const uint64_t off = sl.p_off;
+  const int c = sl.cur;
+  AMCL_CUDA_TRY(cudaMemcpyAsync(pose.data(), b->pose[c].as<float4>() + off, m * 16ull, cudaMemcpyDeviceToHost, s));
+  AMCL_CUDA_TRY(cudaMemcpyAsync(w.data(), b->w[c].as<float>() + off, m * 4ull, cudaMemcpyDeviceToHost, s));
+  AMCL_CUDA_TRY(cudaMemcpyAsync(wp.data(), b->wp[c].as<float>() + off, m * 4ull, cudaMemcpyDeviceToHost, s));
+  AMCL_CUDA_TRY(cudaMemcpyAsync(wr.data(), b->wr[c].as<float>() + off, m * 4ull, cudaMemcpyDeviceToHost, s));
+  AMCL_CUDA_TRY(cudaStreamSynchronize(s));
+  for (uint32_t i = 0; i < m; ++i)
+  {
+    float* q = p7 + 7ull * i;
+    q[0] = pose[i].x;
+    q[1] = pose[i].y;
+    q[2] = pose[i].z;
+    q[3] = pose[i].w;
+    q[4] = w[i];
+    q[5] = wp[i];
+    q[6] = wr[i];
+  }
+  return AMCL_OK;
+}
+
+extern "C" int amcl_batch_stage(amcl_batch_t b, int slot, const float* xyz, uint32_t n, uint32_t stride_floats,
+                                const float* ranges4, uint32_t nr, const double* odom8, double alpha, double sigma,
+                                double roll, double pitch, int resample)
+{
+  if (!b || (n && !xyz) || (nr && !ranges4) || stride_floats < 3)
+    return fail(AMCL_EINVAL, "amcl_batch_stage: bad arguments");
+  if (nr > MAX_RANGES)
+    return fail(AMCL_ERANGE, "amcl_batch_stage: more than 64 range measurements");
+  std::lock_guard<std::mutex> lock(b->mu);
+  int rc = slot_check(b, slot);
+  if (rc)
+    return rc;
+  BatchSlot& sl = b->slots[slot];
+  if (!sl.initialized)
+    return fail(AMCL_ESTATE, "amcl_batch_stage: filter not initialised");
+  sl.cloud.resize(n);
+  pack_cloud(xyz, n, stride_floats, sl.cloud.data());
+  sl.ranges.resize(nr);
+  if (nr)
+    std::memcpy(sl.ranges.data(), ranges4, nr * 16ull);
+  sl.predict = odom8 != nullptr;
+  if (odom8)
+    std::memcpy(sl.odom, odom8, sizeof(sl.odom));
+  sl.alpha = alpha;
+  sl.sigma = sigma;
+  sl.roll = roll;
+  sl.pitch = pitch;
+  sl.resample = resample != 0;
+  sl.staged = true;
+  return AMCL_OK;
+}
+
+extern "C" int amcl_batch_step(amcl_batch_t b)
+{
+  if (!b)
+    return fail(AMCL_EINVAL, "amcl_batch_step: null batch");
+  std::lock_guard<std::mutex> lock(b->mu);
+  int rc;
+  if ((rc = batch_wait(b)))
+    return rc;
+  // table capacity in shared memory: the largest grid among the staged filters
+  uint32_t tab = 0;
+  for (auto& sl : b->slots)
+    if (sl.used && sl.staged && sl.grid && sl.grid->built)
+      tab = std::max<uint32_t>(tab, sl.grid->info.size[0] + sl.grid->info.size[1] + sl.grid->info.size[2] + 3);
+  if ((rc = pack_steps(b)))
+    return rc;
+  if (!b->n_steps)
+    return AMCL_OK;
+  if (tab > b->tab_cap || !b->exec || b->graph_threads != b->threads || b->graph_chunk != b->chunk)
+  {
+    b->tab_cap = std::max(tab, b->tab_cap);
+    const size_t smem = weight_smem(b, b->chunk);
+    if (smem > 227 * 1024)
+      return fail(AMCL_ERANGE, "amcl_batch_step: grid tables and point tile exceed shared memory");
+    AMCL_CUDA_TRY(cudaFuncSetAttribute(k_b_weight, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(smem)));
+    if ((rc = build_graph(b)))
+      return rc;
+  }
+  if ((rc = graph_update_copies(b)))
+    return rc;
+  AMCL_CUDA_TRY(cudaGraphLaunch(b->exec, b->st.s));
+  for (uint32_t si : b->step_slots)
+  {
+    BatchSlot& sl = b->slots[si];
+    if (sl.resample)
+      sl.cur = 1 - sl.cur;
+    sl.stats_valid = false;
+  }
+  b->in_flight = true;
+  b->steps_done += 1;
+  for (int k = 0; k < 7; ++k)  // the graph's kernels
+    count_launch();
+  return AMCL_OK;
+}
+
+extern "C" int amcl_batch_wait(amcl_batch_t b)
+{
+  if (!b)
+    return fail(AMCL_EINVAL, "amcl_batch_wait: null batch");
+  std::lock_guard<std::mutex> lock(b->mu);
+  return batch_wait(b);
+}
+
+extern "C" int amcl_batch_get_mean(amcl_batch_t b, int slot, float mean7[7], double mean_var[8])
+{
+  if (!b || !mean7)
+    return fail(AMCL_EINVAL, "amcl_batch_get_mean: bad arguments");
+  std::lock_guard<std::mutex> lock(b->mu);
+  int rc = slot_check(b, slot);
+  if (rc || (rc = batch_wait(b)))
+    return rc;
+  const PFStats* st = b->h_stats.as<PFStats>() + slot;
+  for (int k = 0; k < 7; ++k)
+    mean7[k] = k < 4 ? st->mean_f[k] : 0.0f;
+  if (mean_var)
+    for (int k = 0; k < 4; ++k)
+    {
+      mean_var[k] = st->mean[k];
+      mean_var[4 + k] = st->var[k];
+    }
+  return AMCL_OK;
+}
+
+extern "C" int amcl_batch_set_tuning(amcl_batch_t b, int threads, int chunk)
+{
+  if (!b || (threads != 64 && threads != 128 && threads != 256 && threads != 512) || chunk < 64 || chunk > 4096 ||
+      chunk % UNROLL)
+    return fail(AMCL_EINVAL, "amcl_batch_set_tuning: threads in {64,128,256,512}, chunk a multiple of 8 in [64,4096]");
+  std::lock_guard<std::mutex> lock(b->mu);
+  b->threads = threads;
+  b->chunk = chunk;
+  return AMCL_OK;
+}
+
+extern "C" int amcl_batch_get_tuning(amcl_batch_t b, int* threads, int* chunk)
+{
+  if (!b || !threads || !chunk)
+    return fail(AMCL_EINVAL, "amcl_batch_get_tuning: bad arguments");
+  *threads = b->threads;
+  *chunk = b->chunk;
+  return AMCL_OK;
+}
+
+extern "C" int amcl_batch_stream(amcl_batch_t b, void** stream)
+{
+  if (!b || !stream)
+    return fail(AMCL_EINVAL, "amcl_batch_stream: bad arguments");
+  *stream = b->st.s;
+  return AMCL_OK;
+}
+
+extern "C" int amcl_batch_capacity(amcl_batch_t b, uint64_t* free_particles, uint32_t* free_slots)
+{
+  if (!b)
+    return fail(AMCL_EINVAL, "amcl_batch_capacity: null batch");
+  std::lock_guard<std::mutex> lock(b->mu);
+  uint64_t fp = 0;
+  for (auto& fr : b->free_ranges)
+    fp = std::max(fp, fr.second);
+  uint32_t fs = 0;
+  for (auto& sl : b->slots)
+    fs += sl.used ? 0 : 1;
+  if (free_particles)
+    *free_particles = fp;
+  if (free_slots)
+    *free_slots = fs;
+  return AMCL_OK;
+}
+
+// ---- autotuner --------------------------------------------------------------------------------
+
+namespace
+{
+void rebuild_weight_items(amcl_batch_s* b, int threads)
+{
+  const SlotStep* hs = b->h_steps.as<SlotStep>();
+  std::vector<std::pair<uint64_t, uint2>> wt;
+  for (uint32_t s = 0; s < b->n_steps; ++s)
+  {
+    const uint32_t ntile = ceil_div(hs[s].P, threads);
+    for (uint32_t k = 0; k < ntile; ++k)
+      wt.push_back({ static_cast<uint64_t>(std::max<uint32_t>(hs[s].N, 1)), make_uint2(s, k) });
+  }
+  std::stable_sort(wt.begin(), wt.end(), [](const std::pair<uint64_t, uint2>& x, const std::pair<uint64_t, uint2>& y) {
+    return x.first > y.first;
+  });
+  uint2* hw = b->h_wt.as<uint2>();
+  for (size_t k = 0; k < wt.size(); ++k)
+    hw[k] = wt[k].second;
+  b->n_wt = static_cast<uint32_t>(wt.size());
+  b->h_counts.as<uint32_t>()[2] = b->n_wt;
+}
+}  // namespace
+
+extern "C" int amcl_batch_autotune(amcl_batch_t b, int reps, int* best_threads, int* best_chunk, double* best_ms)
+{
+  if (!b || reps < 1)
+    return fail(AMCL_EINVAL, "amcl_batch_autotune: bad arguments");
+  std::lock_guard<std::mutex> lock(b->mu);
+  int rc = batch_wait(b);
+  if (rc)
+    return rc;
+  if (!b->n_steps)
+    return fail(AMCL_ESTATE, "amcl_batch_autotune: run at least one step first");
+  cudaStream_t s = b->st.s;
+  const uint64_t cap = b->max_particles;
+  // Save what the weighting kernel overwrites.
+  DevBuf save;
+  const size_t fbytes = cap * 4;
+  if ((rc = save.ensure(4 * fbytes + cap)))
+    return rc;
+  char* sp = save.as<char>();
+  AMCL_CUDA_TRY(cudaMemcpyAsync(sp, b->wp[0].p, fbytes, cudaMemcpyDeviceToDevice, s));
+  AMCL_CUDA_TRY(cudaMemcpyAsync(sp + fbytes, b->wp[1].p, fbytes, cudaMemcpyDeviceToDevice, s));
+  AMCL_CUDA_TRY(cudaMemcpyAsync(sp + 2 * fbytes, b->wr[0].p, fbytes, cudaMemcpyDeviceToDevice, s));
+  AMCL_CUDA_TRY(cudaMemcpyAsync(sp + 3 * fbytes, b->wr[1].p, fbytes, cudaMemcpyDeviceToDevice, s));
+  AMCL_CUDA_TRY(cudaMemcpyAsync(sp + 4 * fbytes, b->inmap.p, cap, cudaMemcpyDeviceToDevice, s));
+  const int cand_t[] = { 128, 256, 512 };
+  const int cand_c[] = { 256, 512, 1024, 2048 };
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  BatchDev d = batch_dev(b);
+  const int sms = device_sm_count();
+  double best = 1e300;
+  int bt = b->threads, bc = b->chunk;
+  for (int t : cand_t)
+  {
+    rebuild_weight_items(b, t);
+    AMCL_CUDA_TRY(cudaMemcpyAsync(b->wt_items.p, b->h_wt.p, std::max<uint64_t>(b->n_wt, 1) * sizeof(uint2),
+                                  cudaMemcpyHostToDevice, s));
+    AMCL_CUDA_TRY(cudaMemcpyAsync(b->counts.p, b->h_counts.p, 16, cudaMemcpyHostToDevice, s));
+    for (int c : cand_c)
+    {
+      const size_t smem = weight_smem(b, c);
+      if (smem > 227 * 1024)
+        continue;
+      AMCL_CUDA_TRY(cudaFuncSetAttribute(k_b_weight, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem)));
+      float total = 0;
+      for (int r = -1; r < reps; ++r)
+      {
+        AMCL_CUDA_TRY(cudaMemsetAsync(b->acc.p, 0, static_cast<size_t>(b->max_filters) * ACC_WORDS * 8, s));
+        AMCL_CUDA_TRY(cudaMemsetAsync(b->counter.p, 0, sizeof(unsigned int), s));
+        cudaEventRecord(e0, s);
+        k_b_weight<<<static_cast<unsigned>(sms * 2), t, smem, s>>>(d, static_cast<uint32_t>(c), b->tab_cap);
+        AMCL_LAUNCH_CHECK("k_b_weight(tune)");
+        cudaEventRecord(e1, s);
+        AMCL_CUDA_TRY(cudaEventSynchronize(e1));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (r >= 0)
+          total += ms;
+      }
+      const double avg = total / reps;
+      if (avg < best)
+      {
+        best = avg;
+        bt = t;
+        bc = c;
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  // Restore the filters' state and the item list of the chosen shape.
+  AMCL_CUDA_TRY(cudaMemcpyAsync(b->wp[0].p, sp, fbytes, cudaMemcpyDeviceToDevice, s));
+  AMCL_CUDA_TRY(cudaMemcpyAsync(b->wp[1].p, sp + fbytes, fbytes, cudaMemcpyDeviceToDevice, s));
+  AMCL_CUDA_TRY(cudaMemcpyAsync(b->wr[0].p, sp + 2 * fbytes, fbytes, cudaMemcpyDeviceToDevice, s));
+  AMCL_CUDA_TRY(cudaMemcpyAsync(b->wr[1].p, sp + 3 * fbytes, fbytes, cudaMemcpyDeviceToDevice, s));
+  AMCL_CUDA_TRY(cudaMemcpyAsync(b->inmap.p, sp + 4 * fbytes, cap, cudaMemcpyDeviceToDevice, s));
+  AMCL_CUDA_TRY(cudaStreamSynchronize(s));
+  b->threads = bt;
+  b->chunk = bc;
+  if (b->exec)
+  {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  if (best_threads)
+    *best_threads = bt;
+  if (best_chunk)
+    *best_chunk = bc;
+  if (best_ms)
+    *best_ms = best;
+  return AMCL_OK;
+}

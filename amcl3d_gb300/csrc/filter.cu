@@ -13,220 +13,43 @@
 #include "bulk.cuh"
 #include "exact.cuh"
 #include "grid.cuh"
+#include "filter_dev.cuh"
 #include "philox.cuh"
 
 using namespace amcl;
 
 namespace
 {
-enum Acc
-{
-  ACC_WP = 0,
-  ACC_WR,
-  ACC_W,
-  ACC_W2,  // sum of the normalised weights
-  ACC_M1,  // 4 accumulators: sum w*x, w*y, w*z, w*a
-  ACC_M2 = ACC_M1 + 4,  // 4 accumulators: sum w*x^2, ...
-  ACC_COUNT = ACC_M2 + 4
-};
-constexpr int NDIG = 10;
-constexpr int NT = 256;  // threads per block of the per-particle kernels
+// ---- single-filter kernels: one block of NT particles each --------------------------------------
 
-struct PFStats
-{
-  double sum_wp, sum_wr, sum_w, sum_w2;
-  double mean[4];
-  double var[4];
-  float mean_f[4];
-  int err;
-  int pad;
-};
-
-__device__ __forceinline__ double acc_value(const unsigned long long* acc, int k)
-{
-  return x320_to_double(x320_from_digits(acc + k * NDIG));
-}
-
-// Exact two-product of floats via FMA: a*b = p + e exactly (e rounded only if it
-// underflows; the oracle rounds the same residual the same way).
-__device__ __forceinline__ void two_prod(float a, float b, float& p, float& e)
-{
-  p = __fmul_rn(a, b);
-  e = __fmaf_rn(a, b, -p);
-}
-
-// Block-wide exact sum of one value per thread added to digits `dst`.
-__device__ __forceinline__ void block_exact_add(X320 v, unsigned long long* dst, X320* s_part)
-{
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  v = x320_warp_sum(v);
-  __syncthreads();
-  if (lane == 0)
-    s_part[wid] = v;
-  __syncthreads();
-  if (wid == 0)
-  {
-    X320 t = lane < nw ? s_part[lane] : x320_zero();
-    t = x320_warp_sum(t);
-    if (lane == 0)
-      x320_atomic_add(dst, t);
-  }
-}
-
-// ---- update: blend (ParticleFilter.cpp:157-180) ------------------------------------------
 __global__ __launch_bounds__(NT) void k_blend(uint32_t n, const uint8_t* __restrict__ inmap, float* __restrict__ wp,
                                              float* __restrict__ wr, float* __restrict__ w, double alpha,
                                              unsigned long long* acc)
 {
   __shared__ double s_sum[2];
   __shared__ X320 s_part[NT / 32];
-  if (threadIdx.x == 0)
-  {
-    s_sum[0] = acc_value(acc, ACC_WP);
-    s_sum[1] = acc_value(acc, ACC_WR);
-  }
-  __syncthreads();
-  const double sp = s_sum[0], sr = s_sum[1];
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  float wv = 0.0f;
-  if (i < n)
-  {
-    // wp /= wtp for every particle, stale values of out-of-map particles included.
-    const float a = sp > 0 ? __double2float_rn(__ddiv_rn(static_cast<double>(wp[i]), sp)) : 0.0f;
-    const float b = sr > 0 ? __double2float_rn(__ddiv_rn(static_cast<double>(wr[i]), sr)) : 0.0f;
-    wp[i] = a;
-    wr[i] = b;
-    if (inmap[i])
-      wv = __double2float_rn(
-          __dadd_rn(__dmul_rn(static_cast<double>(a), alpha), __dmul_rn(static_cast<double>(b), __dsub_rn(1.0, alpha))));
-    w[i] = wv;
-  }
-  block_exact_add(x320_from_float(wv), acc + ACC_W * NDIG, s_part);
+  blend_block(blockIdx.x, n, inmap, wp, wr, w, alpha, acc, s_sum, s_part);
 }
 
-// ---- normalise w, accumulate the mean terms and the per-block resample sums ---------------
-// (ParticleFilter.cpp:182-195 for update, :79-92 for init)
 __global__ __launch_bounds__(NT) void k_normalize(uint32_t n, const float4* __restrict__ pose, float* __restrict__ w,
                                                  unsigned long long* acc, X320* __restrict__ blocksum)
 {
-  __shared__ double s_tot;
+  __shared__ double s_sum[2];
   __shared__ X320 s_part[NT / 32];
-  if (threadIdx.x == 0)
-    s_tot = acc_value(acc, ACC_W);
-  __syncthreads();
-  const double tot = s_tot;
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  float wv = 0.0f;
-  float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (i < n)
-  {
-    wv = tot > 0 ? __double2float_rn(__ddiv_rn(static_cast<double>(w[i]), tot)) : 0.0f;
-    w[i] = wv;
-    p = pose[i];
-  }
-  const X320 xw = x320_from_float(wv);
-  // sum of normalised weights: also the resample block sum
-  {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    X320 v = x320_warp_sum(xw);
-    if (lane == 0)
-      s_part[wid] = v;
-    __syncthreads();
-    if (wid == 0)
-    {
-      X320 t = lane < static_cast<int>(NT / 32) ? s_part[lane] : x320_zero();
-      t = x320_warp_sum(t);
-      if (lane == 0)
-      {
-        blocksum[blockIdx.x] = t;
-        x320_atomic_add(acc + ACC_W2 * NDIG, t);
-      }
-    }
-  }
-  const float c[4] = { p.x, p.y, p.z, p.w };
-#pragma unroll
-  for (int k = 0; k < 4; ++k)
-  {
-    float hi, lo;
-    two_prod(wv, c[k], hi, lo);
-    block_exact_add(x320_add(x320_from_float(hi), x320_from_float(lo)), acc + (ACC_M1 + k) * NDIG, s_part);
-    // w*c^2 = w*(s + t) with c*c = s + t exactly; each product split again.
-    float s, t, h1, l1, h2, l2;
-    two_prod(c[k], c[k], s, t);
-    two_prod(wv, s, h1, l1);
-    two_prod(wv, t, h2, l2);
-    X320 q = x320_add(x320_add(x320_from_float(h1), x320_from_float(l1)),
-                      x320_add(x320_from_float(h2), x320_from_float(l2)));
-    block_exact_add(q, acc + (ACC_M2 + k) * NDIG, s_part);
-  }
+  normalize_block(blockIdx.x, n, pose, w, acc, blocksum, s_sum, s_part);
 }
 
 __global__ void k_finalize_stats(const unsigned long long* acc, PFStats* st)
 {
-  if (threadIdx.x != 0 || blockIdx.x != 0)
-    return;
-  st->sum_wp = acc_value(acc, ACC_WP);
-  st->sum_wr = acc_value(acc, ACC_WR);
-  st->sum_w = acc_value(acc, ACC_W);
-  const double s2 = acc_value(acc, ACC_W2);
-  st->sum_w2 = s2;
-  for (int k = 0; k < 4; ++k)
-  {
-    const double m1 = acc_value(acc, ACC_M1 + k);
-    const double m2 = acc_value(acc, ACC_M2 + k);
-    st->mean[k] = m1;  // the reference's mean is sum w*x of the normalised weights
-    st->mean_f[k] = __double2float_rn(m1);
-    if (s2 > 0)
-    {
-      const double mu = __ddiv_rn(m1, s2);
-      st->var[k] = __dsub_rn(__ddiv_rn(m2, s2), __dmul_rn(mu, mu));
-    }
-    else
-      st->var[k] = 0.0;
-  }
+  if (threadIdx.x == 0 && blockIdx.x == 0)
+    finalize_stats(acc, st);
 }
-
-// ---- predict (ParticleFilter.cpp:97-119) ------------------------------------------------------
-struct PredictArgs
-{
-  uint32_t n;
-  uint32_t seed_lo, seed_hi;
-  uint64_t step;
-  float sx, sy, sz, sa;  // (float) |delta * mod|, the normal_distribution<float> stddev
-  double dx, dy, dz, da;
-  float* draws;  // optional 4 per particle
-};
 
 __global__ __launch_bounds__(NT) void k_predict(float4* __restrict__ pose, PredictArgs a)
 {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n)
-    return;
-  Philox4 c;
-  c.v[0] = i;
-  c.v[1] = static_cast<uint32_t>(a.step);
-  c.v[2] = static_cast<uint32_t>(a.step >> 32);
-  c.v[3] = RNG_TAG_PREDICT;
-  float z[4];
-  normals4(philox4x32_10(c, a.seed_lo, a.seed_hi), z);
-  if (a.draws)
-    reinterpret_cast<float4*>(a.draws)[i] = make_float4(z[0], z[1], z[2], z[3]);
-  float4 p = pose[i];
-  // ranGaussian(0, dev) = z * (float)dev + 0.0f  (normal_distribution<float>)
-  const float gx = fadd(fmul(z[0], a.sx), 0.0f);
-  const float gy = fadd(fmul(z[1], a.sy), 0.0f);
-  const float gz = fadd(fmul(z[2], a.sz), 0.0f);
-  const float ga = fadd(fmul(z[3], a.sa), 0.0f);
-  double sd, cd;
-  sincos(static_cast<double>(p.w), &sd, &cd);
-  const float sa = __double2float_rn(sd), ca = __double2float_rn(cd);
-  const float rx = __double2float_rn(__dadd_rn(a.dx, static_cast<double>(gx)));
-  const float ry = __double2float_rn(__dadd_rn(a.dy, static_cast<double>(gy)));
-  p.x = fadd(p.x, fsub(fmul(ca, rx), fmul(sa, ry)));
-  p.y = fadd(p.y, fadd(fmul(sa, rx), fmul(ca, ry)));
-  p.z = __double2float_rn(__dadd_rn(static_cast<double>(p.z), __dadd_rn(a.dz, static_cast<double>(gz))));
-  p.w = __double2float_rn(__dadd_rn(static_cast<double>(p.w), __dadd_rn(a.da, static_cast<double>(ga))));
-  pose[i] = p;
+  if (i < a.n)
+    predict_particle(i, pose, a);
 }
 
 // ---- init (ParticleFilter.cpp:46-77) ----------------------------------------------------------
@@ -281,83 +104,19 @@ __global__ __launch_bounds__(NT) void k_init(float4* __restrict__ pose, float* _
   block_exact_add(x320_from_float(wv), acc + ACC_W * NDIG, s_part);
 }
 
-// ---- resample (ParticleFilter.cpp:198-222) ---------------------------------------------------
-// u_m = r + factor*m in float; index[m] = first i with C_i >= u_m where C is the
-// inclusive prefix of w; for each particle hi_i = #{m : u_m <= C_i} (u is
-// non-decreasing in m), so index[m] = first i with hi_i > m.
-
-__device__ __forceinline__ float u_of(float r, float factor, uint32_t m) { return fadd(r, fmul(factor, static_cast<float>(m))); }
-
 __global__ __launch_bounds__(NT) void k_block_sums(uint32_t n, const float* __restrict__ w, X320* __restrict__ blocksum)
 {
   __shared__ X320 s_part[NT / 32];
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  X320 v = x320_from_float(i < n ? w[i] : 0.0f);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  v = x320_warp_sum(v);
-  if (lane == 0)
-    s_part[wid] = v;
-  __syncthreads();
-  if (wid == 0)
-  {
-    X320 t = lane < static_cast<int>(NT / 32) ? s_part[lane] : x320_zero();
-    t = x320_warp_sum(t);
-    if (lane == 0)
-      blocksum[blockIdx.x] = t;
-  }
+  block_sum_block(blockIdx.x, n, w, blocksum, s_part);
 }
 
-// Exact inclusive prefix C_i, then hi_i by binary search over m.
 __global__ __launch_bounds__(NT) void k_prefix_hi(uint32_t n, const float* __restrict__ w,
                                                  const X320* __restrict__ blocksum, float r, float factor,
                                                  int32_t* __restrict__ hi)
 {
   __shared__ X320 s_scan[NT / 32];
   __shared__ X320 s_base;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  // exclusive prefix of the block sums before this block
-  if (wid == 0)
-  {
-    X320 t = x320_zero();
-    for (uint32_t b = lane; b < blockIdx.x; b += 32)
-      t = x320_add(t, blocksum[b]);
-    t = x320_warp_sum(t);
-    if (lane == 0)
-      s_base = t;
-  }
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  const X320 own = x320_from_float(i < n ? w[i] : 0.0f);
-  // warp inclusive scan
-  X320 x = own;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1)
-  {
-    X320 y;
-#pragma unroll
-    for (int k = 0; k < 5; ++k)
-      y.w[k] = __shfl_up_sync(0xFFFFFFFFu, x.w[k], o);
-    if (lane >= o)
-      x = x320_add(x, y);
-  }
-  if (lane == 31)
-    s_scan[wid] = x;
-  __syncthreads();
-  X320 c = s_base;
-  for (int k = 0; k < wid; ++k)
-    c = x320_add(c, s_scan[k]);
-  c = x320_add(c, x);  // inclusive prefix C_i
-  if (i >= n)
-    return;
-  uint32_t lo = 0, up = n;
-  while (lo < up)
-  {
-    const uint32_t mid = (lo + up) >> 1;
-    if (x320_cmp(x320_from_float(u_of(r, factor, mid)), c) <= 0)
-      lo = mid + 1;
-    else
-      up = mid;
-  }
-  hi[i] = static_cast<int32_t>(lo);
+  prefix_hi_block(blockIdx.x, n, w, blocksum, r, factor, hi, s_scan, &s_base);
 }
 
 // The reference's float running sum c += w (ParticleFilter.cpp:203,214), one thread.
@@ -399,25 +158,8 @@ __global__ __launch_bounds__(NT) void k_gather(uint32_t n, const int32_t* __rest
                                               int32_t* __restrict__ idx_o)
 {
   const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= n)
-    return;
-  uint32_t lo = 0, up = n;
-  while (lo < up)
-  {
-    const uint32_t mid = (lo + up) >> 1;
-    if (static_cast<uint32_t>(hi[mid]) > m)
-      up = mid;
-    else
-      lo = mid + 1;
-  }
-  // lo == n: the reference runs past its array (reads p_[N]); clamp to the last particle.
-  const uint32_t src = lo < n ? lo : n - 1;
-  pose_o[m] = pose[src];
-  wp_o[m] = wp[src];
-  wr_o[m] = wr[src];
-  w_o[m] = factor;  // new_p[m].w = factor (ParticleFilter.cpp:217)
-  if (idx_o)
-    idx_o[m] = static_cast<int32_t>(src);
+  if (m < n)
+    gather_particle(m, n, hi, pose, wp, wr, pose_o, w_o, wp_o, wr_o, factor, idx_o);
 }
 }  // namespace
 

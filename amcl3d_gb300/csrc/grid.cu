@@ -85,12 +85,18 @@ int grid_prepare_view(amcl_grid_s* g)
   v.step_y = in.size[0];
   v.step_z = in.size[0] * in.size[1];
   v.cells = g->cells();
-  int rc = g->tabs.ensure(g->tabs_host.size() * sizeof(float));
+  // Pairs (T[k], T[k+1]) per axis, T[size+1] = +inf: one 64-bit load settles a cell.
+  std::vector<float2> pairs(g->tabs_host.size());
+  for (int a = 0; a < 3; ++a)
+    for (uint32_t k = 0; k <= in.size[a]; ++k)
+      pairs[v.toff[a] + k] = make_float2(g->tabs_host[v.toff[a] + k],
+                                         k < in.size[a] ? g->tabs_host[v.toff[a] + k + 1] : INFINITY);
+  int rc = g->tabs.ensure(pairs.size() * sizeof(float2));
   if (rc)
     return rc;
-  AMCL_CUDA_TRY(cudaMemcpyAsync(g->tabs.p, g->tabs_host.data(), g->tabs_host.size() * sizeof(float),
-                                cudaMemcpyHostToDevice, g->st.s));
-  v.T = g->tabs.as<float>();
+  AMCL_CUDA_TRY(cudaMemcpyAsync(g->tabs.p, pairs.data(), pairs.size() * sizeof(float2), cudaMemcpyHostToDevice,
+                                g->st.s));
+  v.T2 = g->tabs.as<float2>();
   v.prob_f32 = g->prob.as<float>();
   v.prob_f16 = g->prob16.as<__half>();
   v.prob_u8 = g->prob8.as<uint8_t>();

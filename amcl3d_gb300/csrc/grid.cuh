@@ -13,7 +13,7 @@ struct amcl_grid_s
   amcl::DevBuf prob;    // float per cell (Grid3dCell::prob)
   amcl::DevBuf prob16;  // __half copy
   amcl::DevBuf prob8;   // uint8 copy
-  amcl::DevBuf tabs;    // locate tables (float)
+  amcl::DevBuf tabs;    // locate tables: float2 pairs (T[k], T[k+1]) per axis
   std::vector<float> tabs_host;
   amcl::GridView view{};
   uint64_t cells() const
@@ -50,6 +50,7 @@ struct WeightArgs
   int cloud_sum;  // 0 float running sum, 1 Neumaier
   int kernel;     // 1 thread-per-particle, 2 two-phase
   int ignore_map; // weigh every particle (computeCloudWeight itself has no map test)
+  int yaw_only;   // set by launch_cloud_weight when roll = pitch = 0
   float* scratch;           // two-phase only: ceil(P/32)*32*N floats
   uint64_t scratch_floats;  // capacity
 };

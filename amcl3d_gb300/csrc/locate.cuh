@@ -12,16 +12,25 @@
 //  * the divide/floor/compare chain is replaced by exact float comparisons against a
 //    per-axis table T[k] = the smallest float X with floor(fl64(X / res)) >= k and a
 //    bound V = the smallest float X that fails a bound check (both computed on the
-//    host with the reference's own double arithmetic), so the cell index is decided
-//    by float compares that give exactly the reference's answer;
-//  * the double add is evaluated as a float-float sum (the particle offset split
-//    into H + L, Knuth's two-sum), which lands within one float ulp of the exact
-//    X; when any threshold lies within a safe margin of that estimate the point takes
-//    the exact FP64 path (one double add and a rounding), so every point gets the
-//    reference's X and cell index.
+//    host with the reference's own double arithmetic); the kernels keep the table
+//    as pairs (T[k], T[k+1]) so one 64-bit shared load settles a cell;
+//  * when the particle's offset double(t) - min is exactly a float (always when the
+//    map minimum is 0, and whenever the subtraction happens to be exact), the double
+//    add of two floats followed by the rounding to float is exactly the float add, so
+//    X = s + H in one instruction;
+//  * otherwise the double add is evaluated as a float-float sum (the offset split
+//    into H + L, Knuth's two-sum), which lands within one float ulp of the exact X;
+//    when any threshold lies within a safe margin of that estimate the point takes
+//    the exact FP64 path (one double add and a rounding);
+//  * with roll = pitch = 0 the products with the zero rotation coefficients only ever
+//    change the sign of a zero sum, which moves no point to another cell, so they are
+//    skipped (non-finite points, which those products turn into NaN, are rejected
+//    explicitly instead).
 #pragma once
 #include <cuda_fp16.h>
 #include <stdint.h>
+
+#include "../../include/amcl3d_gpu.h"
 
 namespace amcl
 {
@@ -37,8 +46,8 @@ struct GridView
   uint32_t step_y, step_z;
   // isIntoMap as float compares: x >= lo[a] && x < hi[a]  (Grid3d.cpp:207)
   float in_lo[3], in_hi[3];
-  // locate tables
-  const float* T;  // x: [0, sx], y: [sx+1, sx+sy+1], z: ... (size+1 entries per axis)
+  // locate tables: (T[k], T[k+1]) for k = 0..size (T[size+1] = +inf), per axis at toff[a]
+  const float2* T2;
   uint32_t toff[3];
   float V[3];
   float inv_res[3];
@@ -53,9 +62,9 @@ struct PartXf
   float r[9];
   float H[3], L[3];
   double off[3];
-  // All three offsets are exact floats (L == 0).  Then fl64(s + H) is the exact
-  // sum of two floats, or rounds only bits far below the float rounding point, so
-  // X = fl32(fl64(s + H)) equals the single float add s + H: no estimate needed.
+  // All three offsets are exact floats (off == H): then fl64(s + H) is the exact sum
+  // of two floats, or rounds only bits far below the float rounding point, so
+  // X = fl32(fl64(s + H)) equals the single float add s + H.
   int exact;
 };
 
@@ -101,48 +110,30 @@ __device__ __forceinline__ void make_partxf(const GridView& g, float sr, float c
                 : 0;
 }
 
-// Cell index along one axis for an exact X, -1 when the point is rejected
-// (X < 0, X >= V, NaN).  The float estimate floor(X / res) is within one cell of
-// the reference's floor(fl64(X / res)); the table settles it exactly.
-__device__ __forceinline__ int locate_axis_fast(float X, const float* T, float V, float inv_res, int size)
+// Cell index along one axis for an exact X, -1 when the reference rejects the
+// point (X < 0, X >= V, NaN).  floor(X / res) in float is within one cell of the
+// reference's floor(fl64(X / res)); the pair (T[k], T[k+1]) settles it exactly.
+__device__ __forceinline__ int locate_pair(float X, const float2* T2, float V, float inv_res, int size)
 {
-  if (!(X < V))
-    return -1;
   int k = __float2int_rd(fmul(X, inv_res));
-  k = min(max(k, 0), size - 1);
-  if (X < T[k])
-    k -= 1;  // X < 0 ends at -1 (T[0] = 0)
-  else if (X >= T[k + 1])
-    k += 1;
-  return k;
-}
-
-// Cell index along one axis for an exact X, -1 when the point is rejected.
-__device__ __forceinline__ int locate_axis(float X, const float* T, float V, float inv_res, uint32_t size)
-{
-  if (!(X >= 0.0f) || !(X < V))
-    return -1;
-  int k = __float2int_rz(fmul(X, inv_res));
-  k = min(k, static_cast<int>(size) - 1);
-  if (X < T[k])
-    k -= 1;
-  else if (X >= T[k + 1])
-    k += 1;
-  return k;
+  k = min(max(k, 0), size);
+  const float2 t = T2[k];
+  k = (X < t.x) ? k - 1 : ((X >= t.y) ? k + 1 : k);  // X < 0 ends at -1 (T[0] = 0)
+  return (X < V) ? k : -1;
 }
 
 // True when a threshold lies within m of X (the estimate may then be on the wrong side).
-__device__ __forceinline__ bool near_threshold(float X, int k, const float* T, float V, float m)
+__device__ __forceinline__ bool near_threshold(float X, int k, const float2* T2, float V, float m)
 {
   if (fabsf(X) <= m || fabsf(V - X) <= m)
     return true;
   if (k < 0)
     return false;
-  return (X - T[k] <= m) || (T[k + 1] - X <= m);
+  const float2 t = T2[k];
+  return (X - t.x <= m) || (t.y - X <= m);
 }
 
-// Transformed coordinate, estimated in float-float.  Sets *amb when the exact
-// rounding might classify differently.
+// Transformed coordinate, estimated in float-float; m receives the safe margin.
 __device__ __forceinline__ float xform_axis(float s, float H, float L, float& m)
 {
   const float a = fadd(s, H);
@@ -157,26 +148,50 @@ __device__ __forceinline__ float xform_axis(float s, float H, float L, float& m)
   return X;
 }
 
-// Grid cell index of scan point (px, py, pz0) for the particle, or -1 when the
-// reference skips the point.  pz0 is s.z + 0.0f (Grid3d.cpp:174-176).
-// `tab` points at the locate tables (in shared memory in the kernels).
-__device__ __forceinline__ int64_t cell_of_point(const GridView& g, const float* tab, const PartXf& p, float px,
-                                                 float py, float pz0)
+// uint32 index arithmetic of Grid3d.cpp:187; 0xFFFFFFFF marks a skipped point (a
+// valid index is below the cell count, itself below 2^32).
+__device__ __forceinline__ uint32_t cell_index(const GridView& g, int kx, int ky, int kz)
+{
+  if ((kx | ky | kz) < 0)
+    return 0xFFFFFFFFu;
+  return static_cast<uint32_t>(kx) + static_cast<uint32_t>(ky) * g.step_y + static_cast<uint32_t>(kz) * g.step_z;
+}
+
+// Point-transform modes of the weighting loops.
+enum : int
+{
+  XF_GENERAL = 0,  // any offsets: float-float estimate + exact FP64 fallback
+  XF_EXACT = 1,    // offsets are floats: X = s + H
+  XF_YAW = 2       // offsets are floats and roll = pitch = 0
+};
+
+// Grid cell of scan point (px, py, pz0) for the particle, 0xFFFFFFFF when the
+// reference skips it.  pz0 is s.z + 0.0f (Grid3d.cpp:174-176).  `tab` is the pair
+// table (in shared memory in the kernels).
+template <int MODE>
+__device__ __forceinline__ uint32_t cell_of_point(const GridView& g, const float2* tab, const PartXf& p, float px,
+                                                  float py, float pz0)
 {
   float s[3];
-  s[0] = fadd(fadd(fmul(px, p.r[0]), fmul(py, p.r[1])), fmul(pz0, p.r[2]));
-  s[1] = fadd(fadd(fmul(px, p.r[3]), fmul(py, p.r[4])), fmul(pz0, p.r[5]));
-  s[2] = fadd(fadd(fmul(px, p.r[6]), fmul(py, p.r[7])), fmul(pz0, p.r[8]));
+  if (MODE == XF_YAW)
+  {
+    s[0] = fadd(fmul(px, p.r[0]), fmul(py, p.r[1]));
+    s[1] = fadd(fmul(px, p.r[3]), fmul(py, p.r[4]));
+    s[2] = pz0;
+  }
+  else
+  {
+    s[0] = fadd(fadd(fmul(px, p.r[0]), fmul(py, p.r[1])), fmul(pz0, p.r[2]));
+    s[1] = fadd(fadd(fmul(px, p.r[3]), fmul(py, p.r[4])), fmul(pz0, p.r[5]));
+    s[2] = fadd(fadd(fmul(px, p.r[6]), fmul(py, p.r[7])), fmul(pz0, p.r[8]));
+  }
   int k[3];
-  if (p.exact)
+  if (MODE != XF_GENERAL)
   {
 #pragma unroll
     for (int a = 0; a < 3; ++a)
-      k[a] = locate_axis_fast(fadd(s[a], p.H[a]), tab + g.toff[a], g.V[a], g.inv_res[a], static_cast<int>(g.size[a]));
-    if ((k[0] | k[1] | k[2]) < 0)
-      return -1;
-    return static_cast<int64_t>(static_cast<uint32_t>(k[0]) + static_cast<uint32_t>(k[1]) * g.step_y +
-                                static_cast<uint32_t>(k[2]) * g.step_z);
+      k[a] = locate_pair(fadd(s[a], p.H[a]), tab + g.toff[a], g.V[a], g.inv_res[a], static_cast<int>(g.size[a]));
+    return cell_index(g, k[0], k[1], k[2]);
   }
   bool amb = false;
 #pragma unroll
@@ -184,8 +199,8 @@ __device__ __forceinline__ int64_t cell_of_point(const GridView& g, const float*
   {
     float m;
     const float X = xform_axis(s[a], p.H[a], p.L[a], m);
-    const float* T = tab + g.toff[a];
-    k[a] = locate_axis(X, T, g.V[a], g.inv_res[a], g.size[a]);
+    const float2* T = tab + g.toff[a];
+    k[a] = locate_pair(X, T, g.V[a], g.inv_res[a], static_cast<int>(g.size[a]));
     amb |= near_threshold(X, k[a], T, g.V[a], m);
   }
   if (amb)
@@ -195,15 +210,21 @@ __device__ __forceinline__ int64_t cell_of_point(const GridView& g, const float*
     for (int a = 0; a < 3; ++a)
     {
       const float X = __double2float_rn(__dadd_rn(static_cast<double>(s[a]), p.off[a]));
-      k[a] = locate_axis(X, tab + g.toff[a], g.V[a], g.inv_res[a], g.size[a]);
+      k[a] = locate_pair(X, tab + g.toff[a], g.V[a], g.inv_res[a], static_cast<int>(g.size[a]));
     }
   }
-  if (k[0] < 0 || k[1] < 0 || k[2] < 0)
-    return -1;
-  // uint32 index arithmetic of Grid3d.cpp:187
-  const uint32_t idx = static_cast<uint32_t>(k[0]) + static_cast<uint32_t>(k[1]) * g.step_y +
-                       static_cast<uint32_t>(k[2]) * g.step_z;
-  return static_cast<int64_t>(idx);
+  return cell_index(g, k[0], k[1], k[2]);
+}
+
+// A scan point as staged in shared memory: z + 0.0f applied; in the yaw-only mode a
+// point with a non-finite coordinate becomes NaN (the skipped products would have
+// turned it into NaN).
+__device__ __forceinline__ float4 stage_point(float4 c, bool yaw_only)
+{
+  c.z = fadd(c.z, 0.0f);  // (point->z + error_z), error_z = 0 (Grid3d.cpp:166,174-176)
+  if (yaw_only && !(isfinite(c.x) && isfinite(c.y) && isfinite(c.z)))
+    c.x = __int_as_float(0x7FC00000);
+  return c;
 }
 
 template <int STORAGE>

@@ -17,9 +17,13 @@
 //    bulk-copies its slab through shared memory (cp.async.bulk on an mbarrier
 //    ring) and adds the values in cloud order, so the float sum is the same as the
 //    reference's running sum.
+// Both are issue-bound on the per-point arithmetic (the gathers hit L2), so the
+// point loop is specialised per transform mode (locate.cuh) and chunks are padded
+// with NaN points to a multiple of the unroll so the loop carries no bounds checks.
 #include "bulk.cuh"
 #include "exact.cuh"
 #include "grid.cuh"
+#include "weight_dev.cuh"
 
 using namespace amcl;
 
@@ -27,58 +31,6 @@ namespace
 {
 constexpr int WT_THREADS = 256;
 constexpr int WT_CHUNK = 1024;  // points staged per block iteration (16 KB)
-constexpr int MAX_RANGES = 64;
-
-__device__ __forceinline__ float exp_f32_via_f64(float x) { return __double2float_rn(exp(static_cast<double>(x))); }
-
-// ParticleFilter::computeRangeWeight (ParticleFilter.cpp:224-244), float overloads.
-__device__ __forceinline__ float range_weight(float x, float y, float z, const float4* rg, int nr, float k1, float k2)
-{
-  if (nr == 0)
-    return 0.0f;
-  float w = 1.0f;
-  for (int b = 0; b < nr; ++b)
-  {
-    const float4 R = rg[b];  // (r, ax, ay, az)
-    const float dx = fsub(x, R.y), dy = fsub(y, R.z), dz = fsub(z, R.w);
-    const float r = __fsqrt_rn(fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz)));
-    const float d = fsub(r, R.x);
-    const float e = exp_f32_via_f64(fmul(fmul(-k2, d), d));
-    w = fmul(w, fmul(k1, e));
-  }
-  return w;
-}
-
-// Block-wide exact sums of (a, b) added to the grid-wide digit accumulators.
-__device__ __forceinline__ void block_exact_pair(float va, float vb, bool take, unsigned long long* acc_a,
-                                                 unsigned long long* acc_b, X320* s_part)
-{
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  X320 xa = take ? x320_from_float(va) : x320_zero();
-  X320 xb = take ? x320_from_float(vb) : x320_zero();
-  xa = x320_warp_sum(xa);
-  xb = x320_warp_sum(xb);
-  if (lane == 0)
-  {
-    s_part[2 * wid] = xa;
-    s_part[2 * wid + 1] = xb;
-  }
-  __syncthreads();
-  if (wid == 0)
-  {
-    X320 ta = lane < nw ? s_part[2 * lane] : x320_zero();
-    X320 tb = lane < nw ? s_part[2 * lane + 1] : x320_zero();
-    ta = x320_warp_sum(ta);
-    tb = x320_warp_sum(tb);
-    if (lane == 0)
-    {
-      if (acc_a)
-        x320_atomic_add(acc_a, ta);
-      if (acc_b)
-        x320_atomic_add(acc_b, tb);
-    }
-  }
-}
 
 template <int STORAGE, int SUM>
 __global__ __launch_bounds__(WT_THREADS) void k_weight_fused(WeightArgs a, GridView g)
@@ -87,91 +39,13 @@ __global__ __launch_bounds__(WT_THREADS) void k_weight_fused(WeightArgs a, GridV
   float4* s_pts = reinterpret_cast<float4*>(smem);
   float4* s_rg = s_pts + WT_CHUNK;
   X320* s_part = reinterpret_cast<X320*>(s_rg + MAX_RANGES);
-  float* s_tab = reinterpret_cast<float*>(s_part + 2 * (WT_THREADS / 32));
+  float2* s_tab = reinterpret_cast<float2*>(s_part + 2 * (WT_THREADS / 32));
   // The locate tables are only read per point (a range-only update has no grid).
-  const uint32_t ntab = a.N ? g.size[0] + g.size[1] + g.size[2] + 3 : 0u;
-  for (uint32_t i = threadIdx.x; i < ntab; i += blockDim.x)
-    s_tab[i] = g.T[i];
+  if (a.N)
+    load_tables(g, s_tab);
   for (uint32_t i = threadIdx.x; i < a.nr; i += blockDim.x)
     s_rg[i] = a.ranges[i];
-
-  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool active = p < a.P;
-  float4 pose = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (active)
-    pose = a.pose[p];
-  const bool inm = active && (a.ignore_map || into_map(g, pose.x, pose.y, pose.z));
-  PartXf xf;
-  if (inm)
-    make_partxf(g, a.sr, a.cr, a.sp, a.cp, pose.x, pose.y, pose.z, pose.w, xf);
-
-  float sum = 0.0f, comp = 0.0f;
-  int n = 0;
-  for (uint32_t base = 0; base < a.N; base += WT_CHUNK)
-  {
-    const uint32_t cnt = min(static_cast<uint32_t>(WT_CHUNK), a.N - base);
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x)
-    {
-      float4 c = a.cloud[base + i];
-      c.z = fadd(c.z, 0.0f);  // (point->z + error_z), error_z = 0 (Grid3d.cpp:166,174-176)
-      s_pts[i] = c;
-    }
-    __syncthreads();
-    if (!inm)
-      continue;
-    for (uint32_t k = 0; k < cnt; k += 8)
-    {
-      int64_t cell[8];
-#pragma unroll
-      for (int j = 0; j < 8; ++j)
-      {
-        cell[j] = -1;
-        if (k + j < cnt)
-        {
-          const float4 s = s_pts[k + j];
-          cell[j] = cell_of_point(g, s_tab, xf, s.x, s.y, s.z);
-        }
-      }
-      float v[8];
-#pragma unroll
-      for (int j = 0; j < 8; ++j)
-        v[j] = cell[j] >= 0 ? gather_prob<STORAGE>(g, static_cast<uint32_t>(cell[j])) : 0.0f;
-#pragma unroll
-      for (int j = 0; j < 8; ++j)
-      {
-        if (cell[j] < 0)
-          continue;
-        if (SUM == 0)
-        {
-          sum = fadd(sum, v[j]);  // weight += grid_ptr[grid_index].prob (Grid3d.cpp:191)
-        }
-        else
-        {
-          const float t = fadd(sum, v[j]);
-          comp = fadd(comp, fabsf(sum) >= fabsf(v[j]) ? fadd(fsub(sum, t), v[j]) : fadd(fsub(v[j], t), sum));
-          sum = t;
-        }
-        n += 1;
-      }
-    }
-  }
-  float wpv = 0.0f, wrv = 0.0f;
-  if (inm)
-  {
-    const float tot = SUM == 0 ? sum : fadd(sum, comp);
-    wpv = (n <= 10) ? 0.0f : __fdiv_rn(tot, static_cast<float>(n));  // Grid3d.cpp:198
-    wrv = range_weight(pose.x, pose.y, pose.z, s_rg, static_cast<int>(a.nr), a.k1, a.k2);
-    a.wp[p] = wpv;
-    a.wr[p] = wrv;
-  }
-  if (active && a.inmap)
-    a.inmap[p] = inm ? 1 : 0;
-  if (a.acc_wp || a.acc_wr)
-  {
-    __syncthreads();
-    block_exact_pair(wpv, wrv, inm, a.acc_wp, a.acc_wr, s_part);
-  }
+  weigh_block<STORAGE, SUM>(a, g, blockIdx.x * blockDim.x, WT_CHUNK, s_pts, s_rg, s_part, s_tab);
 }
 
 // ---- two-phase ----------------------------------------------------------------------------
@@ -185,24 +59,48 @@ struct __align__(16) PartRec
   int inm;
 };
 
+template <int STORAGE, int MODE>
+__device__ __forceinline__ void tile_values(const float4* s_pts, uint32_t k0, uint32_t cnt, const float2* s_tab,
+                                            const GridView& g, const PartXf& xf, float* out, uint32_t base)
+{
+  for (uint32_t kk = 0; kk < TP_PTS_PER_WARP; kk += UNROLL)
+  {
+    uint32_t cell[UNROLL];
+#pragma unroll
+    for (int j = 0; j < UNROLL; ++j)
+    {
+      const float4 s = s_pts[k0 + kk + j];
+      cell[j] = cell_of_point<MODE>(g, s_tab, xf, s.x, s.y, s.z);
+    }
+#pragma unroll
+    for (int j = 0; j < UNROLL; ++j)
+    {
+      const uint32_t k = k0 + kk + j;
+      if (k >= cnt)
+        continue;
+      const float v = cell[j] != 0xFFFFFFFFu ? gather_prob<STORAGE>(g, cell[j]) : -1.0f;
+      out[static_cast<uint64_t>(base + k) * 32] = v;
+    }
+  }
+}
+
 template <int STORAGE>
 __global__ __launch_bounds__(TP_WARPS * 32) void k_weight_tile_vals(WeightArgs a, GridView g)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   float4* s_pts = reinterpret_cast<float4*>(smem);
   PartRec* s_rec = reinterpret_cast<PartRec*>(s_pts + TP_PTS_PER_BLOCK);
-  float* s_tab = reinterpret_cast<float*>(s_rec + 32);
-  const uint32_t ntab = g.size[0] + g.size[1] + g.size[2] + 3;
+  float2* s_tab = reinterpret_cast<float2*>(s_rec + 32);
+  const uint32_t ntab = table_entries(g);
   for (uint32_t i = threadIdx.x; i < ntab; i += blockDim.x)
-    s_tab[i] = g.T[i];
+    s_tab[i] = g.T2[i];
   const uint32_t tile = blockIdx.x;
   const uint32_t base = blockIdx.y * TP_PTS_PER_BLOCK;
   const uint32_t cnt = base < a.N ? min(static_cast<uint32_t>(TP_PTS_PER_BLOCK), a.N - base) : 0u;
-  for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x)
+  for (uint32_t i = threadIdx.x; i < TP_PTS_PER_BLOCK; i += blockDim.x)
   {
-    float4 c = a.cloud[base + i];
-    c.z = fadd(c.z, 0.0f);
-    s_pts[i] = c;
+    const float nan = __int_as_float(0x7FC00000);
+    s_pts[i] = i < cnt ? stage_point(a.cloud[base + i], a.yaw_only != 0) : make_float4(nan, nan, nan, 0.0f);
   }
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (wid == 0)
@@ -210,6 +108,7 @@ __global__ __launch_bounds__(TP_WARPS * 32) void k_weight_tile_vals(WeightArgs a
     const uint32_t p = tile * 32 + lane;
     PartRec r;
     r.inm = 0;
+    r.xf.exact = 1;
     if (p < a.P)
     {
       const float4 pose = a.pose[p];
@@ -221,34 +120,17 @@ __global__ __launch_bounds__(TP_WARPS * 32) void k_weight_tile_vals(WeightArgs a
   }
   __syncthreads();
   const PartRec rec = s_rec[lane];
+  const bool warp_exact = __all_sync(0xFFFFFFFFu, rec.xf.exact != 0);
   if (!rec.inm)
     return;
   float* out = a.scratch + (static_cast<uint64_t>(tile) * a.N) * 32 + lane;
   const uint32_t k0 = wid * TP_PTS_PER_WARP;
-  for (uint32_t kk = 0; kk < TP_PTS_PER_WARP; kk += 8)
-  {
-    int64_t cell[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j)
-    {
-      const uint32_t k = k0 + kk + j;
-      cell[j] = -2;
-      if (k < cnt)
-      {
-        const float4 s = s_pts[k];
-        cell[j] = cell_of_point(g, s_tab, rec.xf, s.x, s.y, s.z);
-      }
-    }
-#pragma unroll
-    for (int j = 0; j < 8; ++j)
-    {
-      const uint32_t k = k0 + kk + j;
-      if (cell[j] == -2)
-        continue;
-      const float v = cell[j] >= 0 ? gather_prob<STORAGE>(g, static_cast<uint32_t>(cell[j])) : -1.0f;
-      out[static_cast<uint64_t>(base + k) * 32] = v;
-    }
-  }
+  if (warp_exact && a.yaw_only)
+    tile_values<STORAGE, XF_YAW>(s_pts, k0, cnt, s_tab, g, rec.xf, out, base);
+  else if (warp_exact)
+    tile_values<STORAGE, XF_EXACT>(s_pts, k0, cnt, s_tab, g, rec.xf, out, base);
+  else
+    tile_values<STORAGE, XF_GENERAL>(s_pts, k0, cnt, s_tab, g, rec.xf, out, base);
 }
 
 constexpr int TR_STAGE_PTS = 128;  // points per stage: 128 x 32 lanes x 4 B = 16 KB
@@ -279,8 +161,7 @@ __global__ __launch_bounds__(32) void k_weight_tile_reduce(WeightArgs a, GridVie
   __syncwarp();
   const float* slab = a.scratch + static_cast<uint64_t>(tile) * a.N * 32;
   const uint32_t nst = (a.N + TR_STAGE_PTS - 1) / TR_STAGE_PTS;
-  float sum = 0.0f, comp = 0.0f;
-  int n = 0;
+  CloudSum<SUM> acc;
   bool ok = true;
   if (any && a.N)
   {
@@ -308,19 +189,8 @@ __global__ __launch_bounds__(32) void k_weight_tile_reduce(WeightArgs a, GridVie
         for (uint32_t k = 0; k < pts; ++k)
         {
           const float v = buf[k * 32 + lane];
-          if (v < 0.0f)
-            continue;
-          if (SUM == 0)
-          {
-            sum = fadd(sum, v);
-          }
-          else
-          {
-            const float t = fadd(sum, v);
-            comp = fadd(comp, fabsf(sum) >= fabsf(v) ? fadd(fsub(sum, t), v) : fadd(fsub(v, t), sum));
-            sum = t;
-          }
-          n += 1;
+          if (v >= 0.0f)
+            acc.add(v);
         }
       }
       __syncwarp();
@@ -343,8 +213,7 @@ __global__ __launch_bounds__(32) void k_weight_tile_reduce(WeightArgs a, GridVie
   float wpv = 0.0f, wrv = 0.0f;
   if (inm && ok)
   {
-    const float tot = SUM == 0 ? sum : fadd(sum, comp);
-    wpv = (n <= 10) ? 0.0f : __fdiv_rn(tot, static_cast<float>(n));
+    wpv = acc.weight();
     wrv = range_weight(pose.x, pose.y, pose.z, s_rg, static_cast<int>(a.nr), a.k1, a.k2);
     a.wp[p] = wpv;
     a.wr[p] = wrv;
@@ -364,11 +233,16 @@ __global__ __launch_bounds__(32) void k_weight_tile_reduce(WeightArgs a, GridVie
   }
 }
 
+size_t table_bytes(const GridView& g)
+{
+  return (static_cast<size_t>(g.size[0]) + g.size[1] + g.size[2] + 3) * sizeof(float2);
+}
+
 template <int STORAGE, int SUM>
 int launch_fused(const WeightArgs& a, const GridView& g, cudaStream_t s)
 {
   const size_t smem = WT_CHUNK * sizeof(float4) + MAX_RANGES * sizeof(float4) + 2 * (WT_THREADS / 32) * sizeof(X320) +
-                      (g.size[0] + g.size[1] + g.size[2] + 3) * sizeof(float);
+                      (a.N ? table_bytes(g) : 0);
   static bool attr_done = false;
   if (!attr_done)
   {
@@ -383,8 +257,7 @@ int launch_fused(const WeightArgs& a, const GridView& g, cudaStream_t s)
 template <int STORAGE, int SUM>
 int launch_two_phase(const WeightArgs& a, const GridView& g, cudaStream_t s)
 {
-  const size_t smem1 = TP_PTS_PER_BLOCK * sizeof(float4) + 32 * sizeof(PartRec) +
-                       (g.size[0] + g.size[1] + g.size[2] + 3) * sizeof(float);
+  const size_t smem1 = TP_PTS_PER_BLOCK * sizeof(float4) + 32 * sizeof(PartRec) + table_bytes(g);
   const size_t smem2 = static_cast<size_t>(TR_STAGES) * TR_STAGE_PTS * 32 * sizeof(float);
   static bool attr_done = false;
   if (!attr_done)
@@ -451,8 +324,10 @@ int launch_cloud_weight(amcl_grid_s* g, const WeightArgs& a, cudaStream_t s)
     b.kernel = 1;  // no points: nothing to spread, the fused kernel writes wp = 0
   if (b.kernel == 2 && (!b.scratch || b.scratch_floats < two_phase_scratch_floats(b.P, b.N)))
     return fail(AMCL_EINVAL, "two-phase weighting without a large enough scratch buffer");
-  if (b.N && !g->view.T)
+  if (b.N && !g->view.T2)
     return fail(AMCL_ESTATE, "cloud weighting without a built grid");
+  // roll = pitch = 0 (as the float parameters of computeCloudWeight): yaw-only points.
+  b.yaw_only = (b.sr == 0.0f && b.sp == 0.0f && b.cr == 1.0f && b.cp == 1.0f) ? 1 : 0;
   switch (g->view.storage)
   {
     case AMCL_GRID_F16:

@@ -1,0 +1,189 @@
+// Device helpers of the cloud weighting shared by the single-filter kernels
+// (weight.cu) and the batched kernels (batch.cu).
+#pragma once
+#include "exact.cuh"
+#include "grid.cuh"
+#include "locate.cuh"
+
+namespace amcl
+{
+constexpr int UNROLL = 8;
+constexpr int MAX_RANGES = 64;
+
+__device__ __forceinline__ float exp_f32_via_f64(float x) { return __double2float_rn(exp(static_cast<double>(x))); }
+
+// ParticleFilter::computeRangeWeight (ParticleFilter.cpp:224-244), float overloads.
+__device__ __forceinline__ float range_weight(float x, float y, float z, const float4* rg, int nr, float k1, float k2)
+{
+  if (nr == 0)
+    return 0.0f;
+  float w = 1.0f;
+  for (int b = 0; b < nr; ++b)
+  {
+    const float4 R = rg[b];  // (r, ax, ay, az)
+    const float dx = fsub(x, R.y), dy = fsub(y, R.z), dz = fsub(z, R.w);
+    const float r = __fsqrt_rn(fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz)));
+    const float d = fsub(r, R.x);
+    const float e = exp_f32_via_f64(fmul(fmul(-k2, d), d));
+    w = fmul(w, fmul(k1, e));
+  }
+  return w;
+}
+
+// Running sum of the probabilities: the reference's float `weight += prob`
+// (Grid3d.cpp:191) or a Neumaier-compensated float sum.
+template <int SUM>
+struct CloudSum
+{
+  float sum = 0.0f, comp = 0.0f;
+  int n = 0;
+  __device__ __forceinline__ void add(float v)
+  {
+    if (SUM == 0)
+    {
+      sum = fadd(sum, v);
+    }
+    else
+    {
+      const float t = fadd(sum, v);
+      comp = fadd(comp, fabsf(sum) >= fabsf(v) ? fadd(fsub(sum, t), v) : fadd(fsub(v, t), sum));
+      sum = t;
+    }
+    n += 1;
+  }
+  // Grid3d.cpp:198: 0 with 10 or fewer points, else the mean.
+  __device__ __forceinline__ float weight() const
+  {
+    const float tot = SUM == 0 ? sum : fadd(sum, comp);
+    return (n <= 10) ? 0.0f : __fdiv_rn(tot, static_cast<float>(n));
+  }
+};
+
+// Adds the points [0, cnt) of a staged chunk (cnt a multiple of UNROLL, padding
+// points NaN) in order.
+template <int STORAGE, int SUM, int MODE>
+__device__ __forceinline__ void weigh_chunk(const float4* s_pts, uint32_t cnt, const float2* s_tab, const GridView& g,
+                                            const PartXf& xf, CloudSum<SUM>& acc)
+{
+  for (uint32_t k = 0; k < cnt; k += UNROLL)
+  {
+    uint32_t cell[UNROLL];
+#pragma unroll
+    for (int j = 0; j < UNROLL; ++j)
+    {
+      const float4 s = s_pts[k + j];
+      cell[j] = cell_of_point<MODE>(g, s_tab, xf, s.x, s.y, s.z);
+    }
+    float v[UNROLL];
+#pragma unroll
+    for (int j = 0; j < UNROLL; ++j)
+      v[j] = cell[j] != 0xFFFFFFFFu ? gather_prob<STORAGE>(g, cell[j]) : 0.0f;
+#pragma unroll
+    for (int j = 0; j < UNROLL; ++j)
+      if (cell[j] != 0xFFFFFFFFu)
+        acc.add(v[j]);
+  }
+}
+
+// Block-wide exact sums of (a, b) added to the grid-wide digit accumulators.
+__device__ __forceinline__ void block_exact_pair(float va, float vb, bool take, unsigned long long* acc_a,
+                                                 unsigned long long* acc_b, X320* s_part)
+{
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  X320 xa = take ? x320_from_float(va) : x320_zero();
+  X320 xb = take ? x320_from_float(vb) : x320_zero();
+  xa = x320_warp_sum(xa);
+  xb = x320_warp_sum(xb);
+  if (lane == 0)
+  {
+    s_part[2 * wid] = xa;
+    s_part[2 * wid + 1] = xb;
+  }
+  __syncthreads();
+  if (wid == 0)
+  {
+    X320 ta = lane < nw ? s_part[2 * lane] : x320_zero();
+    X320 tb = lane < nw ? s_part[2 * lane + 1] : x320_zero();
+    ta = x320_warp_sum(ta);
+    tb = x320_warp_sum(tb);
+    if (lane == 0)
+    {
+      if (acc_a)
+        x320_atomic_add(acc_a, ta);
+      if (acc_b)
+        x320_atomic_add(acc_b, tb);
+    }
+  }
+}
+
+__device__ __forceinline__ uint32_t table_entries(const GridView& g) { return g.size[0] + g.size[1] + g.size[2] + 3; }
+
+// Copies the grid's locate pairs into shared memory (all threads of the block).
+__device__ __forceinline__ void load_tables(const GridView& g, float2* s_tab)
+{
+  const uint32_t ntab = table_entries(g);
+  for (uint32_t i = threadIdx.x; i < ntab; i += blockDim.x)
+    s_tab[i] = g.T2[i];
+}
+
+// One block of particles [p0, p0 + blockDim) of one filter, one thread per particle
+// over the whole cloud in cloud order (the fused weighting).  The caller has loaded
+// s_tab (when a.N > 0) and s_rg.  Points are staged `chunk` at a time (a multiple of
+// UNROLL).  Every thread of the block must call this.
+template <int STORAGE, int SUM>
+__device__ __forceinline__ void weigh_block(const WeightArgs& a, const GridView& g, uint32_t p0, uint32_t chunk,
+                                            float4* s_pts, const float4* s_rg, X320* s_part, const float2* s_tab)
+{
+  const uint32_t p = p0 + threadIdx.x;
+  const bool active = p < a.P;
+  float4 pose = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (active)
+    pose = a.pose[p];
+  const bool inm = active && (a.ignore_map || into_map(g, pose.x, pose.y, pose.z));
+  PartXf xf;
+  xf.exact = 1;
+  if (inm)
+    make_partxf(g, a.sr, a.cr, a.sp, a.cp, pose.x, pose.y, pose.z, pose.w, xf);
+  // Transform mode, uniform per warp.
+  const bool warp_exact = __all_sync(0xFFFFFFFFu, xf.exact != 0);
+  const int mode = warp_exact ? (a.yaw_only ? XF_YAW : XF_EXACT) : XF_GENERAL;
+
+  CloudSum<SUM> acc;
+  for (uint32_t base = 0; base < a.N; base += chunk)
+  {
+    const uint32_t cnt = min(chunk, a.N - base);
+    const uint32_t cnt8 = (cnt + UNROLL - 1) / UNROLL * UNROLL;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < cnt8; i += blockDim.x)
+    {
+      const float nan = __int_as_float(0x7FC00000);
+      s_pts[i] = i < cnt ? stage_point(a.cloud[base + i], a.yaw_only != 0) : make_float4(nan, nan, nan, 0.0f);
+    }
+    __syncthreads();
+    if (!inm)
+      continue;
+    if (mode == XF_YAW)
+      weigh_chunk<STORAGE, SUM, XF_YAW>(s_pts, cnt8, s_tab, g, xf, acc);
+    else if (mode == XF_EXACT)
+      weigh_chunk<STORAGE, SUM, XF_EXACT>(s_pts, cnt8, s_tab, g, xf, acc);
+    else
+      weigh_chunk<STORAGE, SUM, XF_GENERAL>(s_pts, cnt8, s_tab, g, xf, acc);
+  }
+  float wpv = 0.0f, wrv = 0.0f;
+  if (inm)
+  {
+    wpv = acc.weight();
+    wrv = range_weight(pose.x, pose.y, pose.z, s_rg, static_cast<int>(a.nr), a.k1, a.k2);
+    a.wp[p] = wpv;
+    a.wr[p] = wrv;
+  }
+  if (active && a.inmap)
+    a.inmap[p] = inm ? 1 : 0;
+  if (a.acc_wp || a.acc_wr)
+  {
+    __syncthreads();
+    block_exact_pair(wpv, wrv, inm, a.acc_wp, a.acc_wr, s_part);
+  }
+}
+
+}  // namespace amcl

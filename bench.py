@@ -280,8 +280,12 @@ def run_ours(args, cfg, rank, world, local_rank):
     total_weights = allreduce_sum(weights, world, dev)
     value = total_weights / (ms_max / 1e3)
 
-    # e2e: host scan per step through the C ABI, mean read back every step
-    for k in range(min(args.warmup, 2)):
+    # e2e: host scan per step through the C ABI, mean read back every step, from the
+    # same particle set and generator state as the device-resident run (the particle
+    # spread, and with it the gather locality, changes as the filter converges).
+    pf.set_particles(parts)
+    pf.set_option(4, seed)
+    for k in range(args.warmup):
         step(k, resident=False)
     torch.cuda.synchronize()
     barrier(world)

@@ -215,6 +215,53 @@ int amcl_pf_get_draws(amcl_pf_t pf, float* out, uint32_t cap_floats);
 /* Debug/parity: the last resample's source index per output particle. */
 int amcl_pf_get_resample_index(amcl_pf_t pf, int32_t* out, uint32_t cap);
 
+/* ---- batches: many filters stepped together ------------------------------------------------
+ * No counterpart in the reference (one filter per node there).  A batch owns fixed
+ * device arenas sized at creation: `max_particles` particles in total over at most
+ * `max_filters` filters, and `max_points_per_step` scan points over all filters of one
+ * step.  Adding a filter that does not fit fails with AMCL_ENOMEM (admission against
+ * the memory budget).  Each filter in a batch computes exactly what a single
+ * amcl_pf_t with the same seed computes (same arithmetic, exact sums), whatever the
+ * other filters in the step.  All calls on one batch must come from one thread at a
+ * time. */
+typedef struct amcl_batch_s* amcl_batch_t;
+
+int amcl_batch_create(amcl_batch_t* out, uint32_t max_filters, uint64_t max_particles, uint64_t max_points_per_step,
+                      void* stream);
+int amcl_batch_destroy(amcl_batch_t b);
+/* A filter slot with room for `capacity` particles on `grid` (may be changed later). */
+int amcl_batch_add(amcl_batch_t b, amcl_grid_t grid, uint32_t capacity, uint64_t seed, int* slot);
+int amcl_batch_remove(amcl_batch_t b, int slot);
+int amcl_batch_set_grid(amcl_batch_t b, int slot, amcl_grid_t grid);
+/* ParticleFilter::init for one slot (as amcl_pf_init). */
+int amcl_batch_init(amcl_batch_t b, int slot, int num_particles, float x, float y, float z, float a, float x_dev,
+                    float y_dev, float z_dev, float a_dev);
+int amcl_batch_set_particles(amcl_batch_t b, int slot, const float* p7, uint32_t n);
+int amcl_batch_get_particles(amcl_batch_t b, int slot, float* p7, uint32_t cap);
+/* Stages one filter step for the next amcl_batch_step: predict with odom8 =
+ * (x_mod, y_mod, z_mod, a_mod, delta_x, delta_y, delta_z, delta_a) unless NULL, then
+ * update with the cloud and ranges (as amcl_pf_update), then resample if `resample`. */
+int amcl_batch_stage(amcl_batch_t b, int slot, const float* xyz, uint32_t n, uint32_t stride_floats,
+                     const float* ranges4, uint32_t nr, const double* odom8, double alpha, double sigma, double roll,
+                     double pitch, int resample);
+/* Launches the staged steps of every filter (one CUDA graph launch); returns before
+ * they finish.  Staging for the next step may proceed meanwhile. */
+int amcl_batch_step(amcl_batch_t b);
+int amcl_batch_wait(amcl_batch_t b);
+/* Mean (and double mean + variance) of a slot's last completed update (waits). */
+int amcl_batch_get_mean(amcl_batch_t b, int slot, float mean7[7], double mean_var[8]);
+/* Shape of the weighting kernel: particle tile (threads per block: 64, 128, 256, 512)
+ * and point tile (scan points staged in shared memory per iteration). */
+int amcl_batch_set_tuning(amcl_batch_t b, int threads, int chunk);
+int amcl_batch_get_tuning(amcl_batch_t b, int* threads, int* chunk);
+/* Times the weighting phase of the last step under each candidate (particle tile x
+ * point tile) shape, `reps` runs each, keeps the fastest and reports it.  The state of
+ * every filter is restored afterwards. */
+int amcl_batch_autotune(amcl_batch_t b, int reps, int* best_threads, int* best_chunk, double* best_ms);
+/* Largest contiguous free particle range and free slots (admission headroom). */
+int amcl_batch_capacity(amcl_batch_t b, uint64_t* free_particles, uint32_t* free_slots);
+int amcl_batch_stream(amcl_batch_t b, void** stream);
+
 /* Raw stream of the handle (cudaStream_t), for callers that time it with events. */
 int amcl_pf_stream(amcl_pf_t pf, void** stream);
 int amcl_grid_stream(amcl_grid_t g, void** stream);
