@@ -96,6 +96,31 @@ _SIGS = {
     "amcl_pf_get_draws": [_vp, _fp, _u32],
     "amcl_pf_get_resample_index": [_vp, C.POINTER(_i32), _u32],
     "amcl_pf_stream": [_vp, C.POINTER(_vp)],
+    "amcl_batch_create": [C.POINTER(_vp), _u32, _u64, _u64, _vp],
+    "amcl_batch_destroy": [_vp],
+    "amcl_batch_add": [_vp, _vp, _u32, _u64, C.POINTER(_int)],
+    "amcl_batch_remove": [_vp, _int],
+    "amcl_batch_set_grid": [_vp, _int, _vp],
+    "amcl_batch_init": [_vp, _int, _int, _f, _f, _f, _f, _f, _f, _f, _f],
+    "amcl_batch_set_particles": [_vp, _int, _fp, _u32],
+    "amcl_batch_get_particles": [_vp, _int, _fp, _u32],
+    "amcl_batch_stage": [_vp, _int, _fp, _u32, _u32, _fp, _u32, _dp, _d, _d, _d, _d, _int],
+    "amcl_batch_step": [_vp],
+    "amcl_batch_wait": [_vp],
+    "amcl_batch_get_mean": [_vp, _int, _fp, _dp],
+    "amcl_batch_set_tuning": [_vp, _int, _int],
+    "amcl_batch_get_tuning": [_vp, C.POINTER(_int), C.POINTER(_int)],
+    "amcl_batch_autotune": [_vp, _int, C.POINTER(_int), C.POINTER(_int), C.POINTER(_d)],
+    "amcl_batch_capacity": [_vp, C.POINTER(_u64), C.POINTER(_u32)],
+    "amcl_batch_stream": [_vp, C.POINTER(_vp)],
+    "amcl_server_create": [C.POINTER(_vp), _u32, _u64, _u64, _vp],
+    "amcl_server_destroy": [_vp],
+    "amcl_server_open_session": [_vp, _vp, _u32, _u64, _int, _fp, C.POINTER(_i64)],
+    "amcl_server_close_session": [_vp, _i64],
+    "amcl_server_submit": [_vp, _i64, _fp, _u32, _u32, _fp, _u32, _dp, _d, _d, _d, _d, _int, C.POINTER(_u64)],
+    "amcl_server_poll": [_vp, _vp, _u32, C.POINTER(_u32)],
+    "amcl_server_stats": [_vp, C.POINTER(_u64), C.POINTER(_u64), C.POINTER(_d), C.POINTER(_u32), C.POINTER(_u32)],
+    "amcl_server_batch": [_vp, C.POINTER(_vp)],
     "amcl_pf_profile": [_vp, _int],
     "amcl_pf_profile_read": [_vp, _dp, C.POINTER(_u64), _int],
 }

@@ -1,0 +1,116 @@
+"""Many particle filters stepped together on one GPU (``amcl_batch_*`` in the C ABI).
+
+``FilterBatch`` owns fixed device arenas (the memory budget filters are admitted
+against); each added filter is a slot that behaves exactly like a ``ParticleFilter``
+with the same seed.  ``stage`` records one filter's next step (predict, update,
+resample); ``step`` launches the staged steps of all filters as one CUDA graph.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+from .filter import Grid3d, Particle, _cloud_array, _ranges_array
+
+
+class FilterBatch:
+    def __init__(self, max_filters: int, max_particles: int, max_points_per_step: int, stream: int | None = None):
+        self._h = C.c_void_p()
+        N.call("amcl_batch_create", C.byref(self._h), int(max_filters), int(max_particles),
+               int(max_points_per_step), C.c_void_p(stream) if stream else None)
+
+    def close(self):
+        if self._h:
+            N.lib.amcl_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, grid: Grid3d | None, capacity: int, seed: int) -> int:
+        """A new filter slot; raises AmclError(AMCL_ENOMEM) when it does not fit."""
+        slot = C.c_int()
+        N.call("amcl_batch_add", self._h, grid.handle if grid is not None else None, int(capacity),
+               int(seed) & (2**64 - 1), C.byref(slot))
+        return slot.value
+
+    def try_add(self, grid: Grid3d | None, capacity: int, seed: int) -> int | None:
+        slot = C.c_int()
+        rc = N.lib.amcl_batch_add(self._h, grid.handle if grid is not None else None, int(capacity),
+                                  int(seed) & (2**64 - 1), C.byref(slot))
+        return slot.value if rc == N.AMCL_OK else None
+
+    def remove(self, slot: int) -> None:
+        N.call("amcl_batch_remove", self._h, int(slot))
+
+    def set_grid(self, slot: int, grid: Grid3d) -> None:
+        N.call("amcl_batch_set_grid", self._h, int(slot), grid.handle)
+
+    def init(self, slot, num_particles, x, y, z, a, xd, yd, zd, ad) -> None:
+        N.call("amcl_batch_init", self._h, int(slot), int(num_particles), float(x), float(y), float(z), float(a),
+               float(xd), float(yd), float(zd), float(ad))
+
+    def set_particles(self, slot: int, p7) -> None:
+        a = np.ascontiguousarray(np.asarray(p7, dtype=np.float32).reshape(-1, 7))
+        N.call("amcl_batch_set_particles", self._h, int(slot), N.fptr(a), a.shape[0])
+
+    def particles(self, slot: int, n: int) -> np.ndarray:
+        out = np.empty((n, 7), np.float32)
+        N.call("amcl_batch_get_particles", self._h, int(slot), N.fptr(out), n)
+        return out
+
+    def stage(self, slot: int, cloud, range_data, odom=None, alpha=0.5, sigma=0.1, roll=0.0, pitch=0.0,
+              resample=True) -> None:
+        """odom: (x_mod, y_mod, z_mod, a_mod, dx, dy, dz, da) to predict first, or None."""
+        pts, stride = _cloud_array(cloud)
+        rg = _ranges_array(range_data)
+        od = None if odom is None else np.ascontiguousarray(odom, dtype=np.float64)
+        N.call("amcl_batch_stage", self._h, int(slot), N.fptr(pts), pts.shape[0], stride,
+               N.fptr(rg) if rg.size else None, rg.shape[0], N.dptr(od) if od is not None else None, float(alpha),
+               float(sigma), float(roll), float(pitch), 1 if resample else 0)
+
+    def step(self) -> None:
+        N.call("amcl_batch_step", self._h)
+
+    def wait(self) -> None:
+        N.call("amcl_batch_wait", self._h)
+
+    def getMean(self, slot: int) -> Particle:
+        m = np.zeros(7, np.float32)
+        N.call("amcl_batch_get_mean", self._h, int(slot), N.fptr(m), None)
+        return Particle(*[float(v) for v in m])
+
+    def mean_var(self, slot: int):
+        m = np.zeros(7, np.float32)
+        mv = np.zeros(8, np.float64)
+        N.call("amcl_batch_get_mean", self._h, int(slot), N.fptr(m), N.dptr(mv))
+        return m[:4].copy(), mv[:4].copy(), mv[4:].copy()
+
+    def set_tuning(self, threads: int, chunk: int) -> None:
+        N.call("amcl_batch_set_tuning", self._h, int(threads), int(chunk))
+
+    def tuning(self) -> tuple[int, int]:
+        t, c = C.c_int(), C.c_int()
+        N.call("amcl_batch_get_tuning", self._h, C.byref(t), C.byref(c))
+        return t.value, c.value
+
+    def autotune(self, reps: int = 3) -> tuple[int, int, float]:
+        t, c, ms = C.c_int(), C.c_int(), C.c_double()
+        N.call("amcl_batch_autotune", self._h, int(reps), C.byref(t), C.byref(c), C.byref(ms))
+        return t.value, c.value, ms.value
+
+    def capacity(self) -> tuple[int, int]:
+        fp, fs = C.c_uint64(), C.c_uint32()
+        N.call("amcl_batch_capacity", self._h, C.byref(fp), C.byref(fs))
+        return int(fp.value), int(fs.value)
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        N.call("amcl_batch_stream", self._h, C.byref(s))
+        return int(s.value or 0)

@@ -69,10 +69,10 @@ struct BatchDev
   const float4* cloud;
   const float4* ranges;
   const SlotStep* steps;
-  const uint32_t* counts;  // [0] steps, [1] block items, [2] weight items
+  const uint32_t* counts;  // [0] steps, [1] block items, [2] weight items, [4+2c, 5+2c) class c's item range
   const uint2* blk_items;  // (step, local block)
   const uint2* wt_items;   // (step, particle tile)
-  unsigned int* counter;   // weighting work queue
+  unsigned int* counter;   // weighting work queues, one per class
 };
 
 constexpr int GRID_BLOCKS_PER_SM = 4;
@@ -117,8 +117,13 @@ __device__ __forceinline__ void b_weigh(const BatchDev& d, const SlotStep& st, u
   weigh_block<STORAGE, SUM>(a, st.g, tile * blockDim.x, chunk, s_pts, s_rg, s_part, s_tab);
 }
 
-// Persistent: blocks take (filter, particle tile) items until the queue is empty.
-__global__ void k_b_weight(BatchDev d, uint32_t chunk, uint32_t tab_cap)
+// Persistent: blocks take (filter, particle tile) items of one (storage, sum) class
+// until that class's queue is empty.
+constexpr int N_CLASSES = 6;  // 3 storages x 2 sum modes
+__host__ __device__ inline int weight_class(int storage, int cloud_sum) { return storage * 2 + (cloud_sum ? 1 : 0); }
+
+template <int STORAGE, int SUM>
+__global__ __launch_bounds__(512) void k_b_weight(BatchDev d, uint32_t chunk, uint32_t tab_cap)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   float4* s_pts = reinterpret_cast<float4*>(smem);
@@ -127,17 +132,18 @@ __global__ void k_b_weight(BatchDev d, uint32_t chunk, uint32_t tab_cap)
   float2* s_tab = reinterpret_cast<float2*>(s_part + 2 * 32);
   __shared__ uint32_t s_item;
   __shared__ int s_loaded;
-  const uint32_t nitems = d.counts[2];
+  constexpr int cls = STORAGE * 2 + SUM;
+  const uint32_t begin = d.counts[4 + 2 * cls], end = d.counts[5 + 2 * cls];
   if (threadIdx.x == 0)
     s_loaded = -1;
   while (true)
   {
     __syncthreads();
     if (threadIdx.x == 0)
-      s_item = atomicAdd(d.counter, 1u);
+      s_item = begin + atomicAdd(d.counter + cls, 1u);
     __syncthreads();
     const uint32_t it = s_item;
-    if (it >= nitems)
+    if (it >= end)
       break;
     const uint2 wi = d.wt_items[it];
     const SlotStep& st = d.steps[wi.x];
@@ -151,25 +157,7 @@ __global__ void k_b_weight(BatchDev d, uint32_t chunk, uint32_t tab_cap)
       if (threadIdx.x == 0)
         s_loaded = static_cast<int>(wi.x);
     }
-    const int storage = st.g.storage;
-    if (st.cloud_sum == 0)
-    {
-      if (storage == AMCL_GRID_F16)
-        b_weigh<AMCL_GRID_F16, 0>(d, st, wi.y, chunk, s_pts, s_rg, s_part, s_tab);
-      else if (storage == AMCL_GRID_U8)
-        b_weigh<AMCL_GRID_U8, 0>(d, st, wi.y, chunk, s_pts, s_rg, s_part, s_tab);
-      else
-        b_weigh<AMCL_GRID_F32, 0>(d, st, wi.y, chunk, s_pts, s_rg, s_part, s_tab);
-    }
-    else
-    {
-      if (storage == AMCL_GRID_F16)
-        b_weigh<AMCL_GRID_F16, 1>(d, st, wi.y, chunk, s_pts, s_rg, s_part, s_tab);
-      else if (storage == AMCL_GRID_U8)
-        b_weigh<AMCL_GRID_U8, 1>(d, st, wi.y, chunk, s_pts, s_rg, s_part, s_tab);
-      else
-        b_weigh<AMCL_GRID_F32, 1>(d, st, wi.y, chunk, s_pts, s_rg, s_part, s_tab);
-    }
+    b_weigh<STORAGE, SUM>(d, st, wi.y, chunk, s_pts, s_rg, s_part, s_tab);
   }
 }
 
@@ -344,6 +332,39 @@ size_t weight_smem(const amcl_batch_s* b, int chunk)
          static_cast<size_t>(b->tab_cap) * sizeof(float2);
 }
 
+// One persistent launch per (storage, sum) class; classes without items exit at once.
+int launch_weight_classes(amcl_batch_s* b, const BatchDev& d, int threads, int chunk, cudaStream_t s)
+{
+  const unsigned grid = static_cast<unsigned>(device_sm_count() * 2);
+  const size_t smem = weight_smem(b, chunk);
+  const uint32_t c = static_cast<uint32_t>(chunk);
+  k_b_weight<AMCL_GRID_F32, 0><<<grid, threads, smem, s>>>(d, c, b->tab_cap);
+  k_b_weight<AMCL_GRID_F32, 1><<<grid, threads, smem, s>>>(d, c, b->tab_cap);
+  k_b_weight<AMCL_GRID_F16, 0><<<grid, threads, smem, s>>>(d, c, b->tab_cap);
+  k_b_weight<AMCL_GRID_F16, 1><<<grid, threads, smem, s>>>(d, c, b->tab_cap);
+  k_b_weight<AMCL_GRID_U8, 0><<<grid, threads, smem, s>>>(d, c, b->tab_cap);
+  k_b_weight<AMCL_GRID_U8, 1><<<grid, threads, smem, s>>>(d, c, b->tab_cap);
+  AMCL_LAUNCH_CHECK("k_b_weight");
+  return AMCL_OK;
+}
+
+int set_weight_smem(size_t smem)
+{
+  AMCL_CUDA_TRY(cudaFuncSetAttribute(k_b_weight<AMCL_GRID_F32, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(smem)));
+  AMCL_CUDA_TRY(cudaFuncSetAttribute(k_b_weight<AMCL_GRID_F32, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(smem)));
+  AMCL_CUDA_TRY(cudaFuncSetAttribute(k_b_weight<AMCL_GRID_F16, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(smem)));
+  AMCL_CUDA_TRY(cudaFuncSetAttribute(k_b_weight<AMCL_GRID_F16, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(smem)));
+  AMCL_CUDA_TRY(cudaFuncSetAttribute(k_b_weight<AMCL_GRID_U8, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(smem)));
+  AMCL_CUDA_TRY(cudaFuncSetAttribute(k_b_weight<AMCL_GRID_U8, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(smem)));
+  return AMCL_OK;
+}
+
 // Enqueues the whole step on the batch stream (also what the graph captures).
 int enqueue_step(amcl_batch_s* b, int threads, int chunk, bool copies)
 {
@@ -353,7 +374,7 @@ int enqueue_step(amcl_batch_s* b, int threads, int chunk, bool copies)
   const unsigned grid = static_cast<unsigned>(sms * GRID_BLOCKS_PER_SM);
   if (copies)
   {
-    AMCL_CUDA_TRY(cudaMemcpyAsync(b->counts.p, b->h_counts.p, 4 * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    AMCL_CUDA_TRY(cudaMemcpyAsync(b->counts.p, b->h_counts.p, 16 * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
     AMCL_CUDA_TRY(cudaMemcpyAsync(b->steps.p, b->h_steps.p, std::max<uint64_t>(b->n_steps, 1) * sizeof(SlotStep),
                                   cudaMemcpyHostToDevice, s));
     AMCL_CUDA_TRY(cudaMemcpyAsync(b->blk_items.p, b->h_blk.p, std::max<uint64_t>(b->n_blk, 1) * sizeof(uint2),
@@ -368,10 +389,10 @@ int enqueue_step(amcl_batch_s* b, int threads, int chunk, bool copies)
   k_b_predict<<<grid, NT, 0, s>>>(d);
   AMCL_LAUNCH_CHECK("k_b_predict");
   AMCL_CUDA_TRY(cudaMemsetAsync(b->acc.p, 0, static_cast<size_t>(b->max_filters) * ACC_WORDS * 8, s));
-  AMCL_CUDA_TRY(cudaMemsetAsync(b->counter.p, 0, sizeof(unsigned int), s));
-  k_b_weight<<<static_cast<unsigned>(sms * 2), threads, weight_smem(b, chunk), s>>>(d, static_cast<uint32_t>(chunk),
-                                                                                   b->tab_cap);
-  AMCL_LAUNCH_CHECK("k_b_weight");
+  AMCL_CUDA_TRY(cudaMemsetAsync(b->counter.p, 0, N_CLASSES * sizeof(unsigned int), s));
+  int rc = launch_weight_classes(b, d, threads, chunk, s);
+  if (rc)
+    return rc;
   k_b_blend<<<grid, NT, 0, s>>>(d);
   AMCL_LAUNCH_CHECK("k_b_blend");
   k_b_normalize<<<grid, NT, 0, s>>>(d);
@@ -388,17 +409,55 @@ int enqueue_step(amcl_batch_s* b, int threads, int chunk, bool copies)
   return AMCL_OK;
 }
 
+// Weighting work items of the packed steps: (step, particle tile of `threads`),
+// grouped by (storage, sum) class, longest scans first within a class (stable, so a
+// filter's tiles stay adjacent and reuse the staged tables); class c's range goes to
+// counts[4 + 2c], counts[5 + 2c].
+void build_weight_items(amcl_batch_s* b, int threads)
+{
+  const SlotStep* hs = b->h_steps.as<SlotStep>();
+  struct Item
+  {
+    int cls;
+    uint32_t cost;
+    uint2 it;
+  };
+  std::vector<Item> wt;
+  for (uint32_t s = 0; s < b->n_steps; ++s)
+  {
+    const int cls = weight_class(hs[s].g.storage, static_cast<int>(hs[s].cloud_sum));
+    const uint32_t ntile = ceil_div(hs[s].P, threads);
+    for (uint32_t k = 0; k < ntile; ++k)
+      wt.push_back({ cls, std::max<uint32_t>(hs[s].N, 1), make_uint2(s, k) });
+  }
+  std::stable_sort(wt.begin(), wt.end(), [](const Item& x, const Item& y) {
+    return x.cls != y.cls ? x.cls < y.cls : x.cost > y.cost;
+  });
+  uint2* hw = b->h_wt.as<uint2>();
+  uint32_t* hcnt = b->h_counts.as<uint32_t>();
+  for (int c = 0; c < N_CLASSES; ++c)
+    hcnt[4 + 2 * c] = hcnt[5 + 2 * c] = 0;
+  for (size_t k = 0; k < wt.size(); ++k)
+  {
+    hw[k] = wt[k].it;
+    const int c = wt[k].cls;
+    if (k == 0 || wt[k - 1].cls != c)
+      hcnt[4 + 2 * c] = static_cast<uint32_t>(k);
+    hcnt[5 + 2 * c] = static_cast<uint32_t>(k + 1);
+  }
+  b->n_wt = static_cast<uint32_t>(wt.size());
+  hcnt[2] = b->n_wt;
+}
+
 // Packs the staged steps of every slot into the pinned staging buffers.
 int pack_steps(amcl_batch_s* b)
 {
   SlotStep* hs = b->h_steps.as<SlotStep>();
   uint2* hb = b->h_blk.as<uint2>();
-  uint2* hw = b->h_wt.as<uint2>();
   float4* hc = b->h_cloud.as<float4>();
   float4* hr = b->h_ranges.as<float4>();
   uint32_t ns = 0, nb = 0;
   uint64_t nc = 0, nr = 0;
-  std::vector<std::pair<uint64_t, uint2>> wt;  // (cost, item)
   b->step_slots.clear();
   const int threads = b->threads;
   for (uint32_t si = 0; si < b->slots.size(); ++si)
@@ -478,29 +537,19 @@ int pack_steps(amcl_batch_s* b)
     const uint32_t nblk = ceil_div(sl.P, NT);
     for (uint32_t k = 0; k < nblk; ++k)
       hb[nb++] = make_uint2(ns, k);
-    const uint32_t ntile = ceil_div(sl.P, threads);
-    for (uint32_t k = 0; k < ntile; ++k)
-      wt.push_back({ static_cast<uint64_t>(std::max<uint32_t>(st.N, 1)), make_uint2(ns, k) });
     hs[ns++] = st;
     b->step_slots.push_back(si);
     sl.staged = false;
   }
-  // longest items first (stable: items of one filter stay together for table reuse)
-  std::stable_sort(wt.begin(), wt.end(), [](const std::pair<uint64_t, uint2>& x, const std::pair<uint64_t, uint2>& y) {
-    return x.first > y.first;
-  });
-  for (size_t k = 0; k < wt.size(); ++k)
-    hw[k] = wt[k].second;
   b->n_steps = ns;
   b->n_blk = nb;
-  b->n_wt = static_cast<uint32_t>(wt.size());
   b->n_cloud = nc;
   b->n_ranges = nr;
   uint32_t* hcnt = b->h_counts.as<uint32_t>();
   hcnt[0] = ns;
   hcnt[1] = nb;
-  hcnt[2] = b->n_wt;
   hcnt[3] = 0;
+  build_weight_items(b, threads);
   return AMCL_OK;
 }
 
@@ -681,11 +730,11 @@ extern "C" int amcl_batch_create(amcl_batch_t* out, uint32_t max_filters, uint64
         (rc = b->stats.ensure(static_cast<size_t>(max_filters) * sizeof(PFStats))) ||
         (rc = b->cloud.ensure(pts * 16)) || (rc = b->ranges.ensure(rng * 16)) ||
         (rc = b->steps.ensure(static_cast<size_t>(max_filters) * sizeof(SlotStep))) ||
-        (rc = b->counts.ensure(16)) || (rc = b->blk_items.ensure((cap / NT + max_filters) * sizeof(uint2))) ||
-        (rc = b->wt_items.ensure(items * sizeof(uint2))) || (rc = b->counter.ensure(16)) ||
+        (rc = b->counts.ensure(64)) || (rc = b->blk_items.ensure((cap / NT + max_filters) * sizeof(uint2))) ||
+        (rc = b->wt_items.ensure(items * sizeof(uint2))) || (rc = b->counter.ensure(64)) ||
         (rc = b->h_cloud.ensure(pts * 16)) || (rc = b->h_ranges.ensure(rng * 16)) ||
         (rc = b->h_steps.ensure(static_cast<size_t>(max_filters) * sizeof(SlotStep))) ||
-        (rc = b->h_counts.ensure(16)) || (rc = b->h_blk.ensure((cap / NT + max_filters) * sizeof(uint2))) ||
+        (rc = b->h_counts.ensure(64)) || (rc = b->h_blk.ensure((cap / NT + max_filters) * sizeof(uint2))) ||
         (rc = b->h_wt.ensure(items * sizeof(uint2))) ||
         (rc = b->h_stats.ensure(static_cast<size_t>(max_filters) * sizeof(PFStats)));
   if (!rc && cudaMemsetAsync(b->stats.p, 0, static_cast<size_t>(max_filters) * sizeof(PFStats), b->st.s) != cudaSuccess)
@@ -957,8 +1006,8 @@ extern "C" int amcl_batch_step(amcl_batch_t b)
     const size_t smem = weight_smem(b, b->chunk);
     if (smem > 227 * 1024)
       return fail(AMCL_ERANGE, "amcl_batch_step: grid tables and point tile exceed shared memory");
-    AMCL_CUDA_TRY(cudaFuncSetAttribute(k_b_weight, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(smem)));
+    if ((rc = set_weight_smem(smem)))
+      return rc;
     if ((rc = build_graph(b)))
       return rc;
   }
@@ -1057,25 +1106,6 @@ extern "C" int amcl_batch_capacity(amcl_batch_t b, uint64_t* free_particles, uin
 
 namespace
 {
-void rebuild_weight_items(amcl_batch_s* b, int threads)
-{
-  const SlotStep* hs = b->h_steps.as<SlotStep>();
-  std::vector<std::pair<uint64_t, uint2>> wt;
-  for (uint32_t s = 0; s < b->n_steps; ++s)
-  {
-    const uint32_t ntile = ceil_div(hs[s].P, threads);
-    for (uint32_t k = 0; k < ntile; ++k)
-      wt.push_back({ static_cast<uint64_t>(std::max<uint32_t>(hs[s].N, 1)), make_uint2(s, k) });
-  }
-  std::stable_sort(wt.begin(), wt.end(), [](const std::pair<uint64_t, uint2>& x, const std::pair<uint64_t, uint2>& y) {
-    return x.first > y.first;
-  });
-  uint2* hw = b->h_wt.as<uint2>();
-  for (size_t k = 0; k < wt.size(); ++k)
-    hw[k] = wt[k].second;
-  b->n_wt = static_cast<uint32_t>(wt.size());
-  b->h_counts.as<uint32_t>()[2] = b->n_wt;
-}
 }  // namespace
 
 extern "C" int amcl_batch_autotune(amcl_batch_t b, int reps, int* best_threads, int* best_chunk, double* best_ms)
@@ -1112,25 +1142,25 @@ extern "C" int amcl_batch_autotune(amcl_batch_t b, int reps, int* best_threads, 
   int bt = b->threads, bc = b->chunk;
   for (int t : cand_t)
   {
-    rebuild_weight_items(b, t);
+    build_weight_items(b, t);
     AMCL_CUDA_TRY(cudaMemcpyAsync(b->wt_items.p, b->h_wt.p, std::max<uint64_t>(b->n_wt, 1) * sizeof(uint2),
                                   cudaMemcpyHostToDevice, s));
-    AMCL_CUDA_TRY(cudaMemcpyAsync(b->counts.p, b->h_counts.p, 16, cudaMemcpyHostToDevice, s));
+    AMCL_CUDA_TRY(cudaMemcpyAsync(b->counts.p, b->h_counts.p, 64, cudaMemcpyHostToDevice, s));
     for (int c : cand_c)
     {
       const size_t smem = weight_smem(b, c);
       if (smem > 227 * 1024)
         continue;
-      AMCL_CUDA_TRY(cudaFuncSetAttribute(k_b_weight, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem)));
+      if ((rc = set_weight_smem(smem)))
+        return rc;
       float total = 0;
       for (int r = -1; r < reps; ++r)
       {
         AMCL_CUDA_TRY(cudaMemsetAsync(b->acc.p, 0, static_cast<size_t>(b->max_filters) * ACC_WORDS * 8, s));
-        AMCL_CUDA_TRY(cudaMemsetAsync(b->counter.p, 0, sizeof(unsigned int), s));
+        AMCL_CUDA_TRY(cudaMemsetAsync(b->counter.p, 0, N_CLASSES * sizeof(unsigned int), s));
         cudaEventRecord(e0, s);
-        k_b_weight<<<static_cast<unsigned>(sms * 2), t, smem, s>>>(d, static_cast<uint32_t>(c), b->tab_cap);
-        AMCL_LAUNCH_CHECK("k_b_weight(tune)");
+        if ((rc = launch_weight_classes(b, d, t, c, s)))
+          return rc;
         cudaEventRecord(e1, s);
         AMCL_CUDA_TRY(cudaEventSynchronize(e1));
         float ms = 0;

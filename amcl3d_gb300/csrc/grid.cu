@@ -77,6 +77,7 @@ int grid_prepare_view(amcl_grid_s* g)
     const float Tsz = g->tabs_host[off + in.size[a]];
     v.V[a] = std::min(U, Tsz);
     v.inv_res[a] = static_cast<float>(1.0 / in.resolution);
+    v.eps[a] = static_cast<float>((static_cast<double>(in.size[a]) + 2.0) * std::ldexp(1.0, -22));
     v.min[a] = in.min[a];
     v.in_lo[a] = float_ceil(in.min[a]);
     v.in_hi[a] = float_ceil(in.max[a]);

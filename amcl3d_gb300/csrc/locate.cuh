@@ -51,6 +51,7 @@ struct GridView
   uint32_t toff[3];
   float V[3];
   float inv_res[3];
+  float eps[3];  // boundary margin of locate_fast: (size + 2) * 2^-22
   double min[3];
   uint64_t cells;
   int built;
@@ -122,6 +123,24 @@ __device__ __forceinline__ int locate_pair(float X, const float2* T2, float V, f
   return (X < V) ? k : -1;
 }
 
+// Same result as locate_pair, reading the table only near a cell boundary.
+// q = fl32(X * fl32(1/res)) is within |q| * 2^-23 of X / res, and the reference's
+// floor(fl64(X / res)) differs from floor(X / res) only within 2^-53 relative of an
+// integer; so when frac(q) is at least eps = (size + 2) * 2^-22 away from 0 and 1,
+// floor(q) is the reference's cell.  Otherwise (about 2 eps of the points per axis)
+// the pair table settles it.  X < V and k >= 0 are the reference's bound checks
+// (X < 0 gives k < 0; NaN fails X < V).
+__device__ __forceinline__ int locate_fast(float X, const float2* T2, float V, float inv_res, int size, float eps)
+{
+  const float q = fmul(X, inv_res);
+  const float fl = floorf(q);
+  const float fr = fsub(q, fl);
+  int k = __float2int_rz(fl);
+  if (fr < eps || fr > 1.0f - eps)
+    k = locate_pair(X, T2, V, inv_res, size);
+  return (X < V && k >= 0) ? k : -1;
+}
+
 // True when a threshold lies within m of X (the estimate may then be on the wrong side).
 __device__ __forceinline__ bool near_threshold(float X, int k, const float2* T2, float V, float m)
 {
@@ -190,7 +209,8 @@ __device__ __forceinline__ uint32_t cell_of_point(const GridView& g, const float
   {
 #pragma unroll
     for (int a = 0; a < 3; ++a)
-      k[a] = locate_pair(fadd(s[a], p.H[a]), tab + g.toff[a], g.V[a], g.inv_res[a], static_cast<int>(g.size[a]));
+      k[a] = locate_fast(fadd(s[a], p.H[a]), tab + g.toff[a], g.V[a], g.inv_res[a], static_cast<int>(g.size[a]),
+                         g.eps[a]);
     return cell_index(g, k[0], k[1], k[2]);
   }
   bool amb = false;

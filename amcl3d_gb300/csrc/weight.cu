@@ -33,7 +33,7 @@ constexpr int WT_THREADS = 256;
 constexpr int WT_CHUNK = 1024;  // points staged per block iteration (16 KB)
 
 template <int STORAGE, int SUM>
-__global__ __launch_bounds__(WT_THREADS) void k_weight_fused(WeightArgs a, GridView g)
+__global__ __launch_bounds__(WT_THREADS, 4) void k_weight_fused(WeightArgs a, GridView g)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   float4* s_pts = reinterpret_cast<float4*>(smem);

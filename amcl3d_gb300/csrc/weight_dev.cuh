@@ -7,7 +7,7 @@
 
 namespace amcl
 {
-constexpr int UNROLL = 8;
+constexpr int UNROLL = 4;
 constexpr int MAX_RANGES = 64;
 
 __device__ __forceinline__ float exp_f32_via_f64(float x) { return __double2float_rn(exp(static_cast<double>(x))); }

@@ -327,7 +327,73 @@ def run_ours(args, cfg, rank, world, local_rank):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         rate, desc = cpu_baseline(occ_points, info, scans, ranges, parts, seconds=args.cpu_seconds, gpu_grid=G)
         res["cpu_baseline"] = {"value": rate, "unit": UNIT, **desc}
+    if rank == 0 and world == 1 and args.served_sessions > 0:
+        # p50/p99 update latency, served vs plain, on this GPU: sessions on this map and a room
+        room = S.make_map(seed + 7, size_m=(20.0, 20.0, 5.0), n_boxes=40)
+        G_room = A.Grid3d()
+        G_room.buildGridMap(room.points, room.min, room.max, room.res, S.SENSOR_DEV)
+        wh = S.make_map(seed, size_m=cfg["size_m"], res=0.05, n_boxes=cfg["n_boxes"], box_range=cfg["box_range"],
+                        max_box_height=cfg["max_box_height"])
+        del pf
+        res["served"] = served_vs_plain([G_room, G], [room, wh], args.served_sessions, 10.0, 8.0, 5.0)
     return res
+
+
+def served_vs_plain(grids, maps, n_sessions, rate_hz, duration_s, churn_per_s, seed=7,
+                    p_range=(1000, 100000), n_range=(500, 10000), plain_requests=400):
+    """Sessions served with continuous batching vs the same request mix one filter per
+    call, on the same GPU.  Returns the "served" JSON object."""
+    from amcl3d_gb300 import serve as SV
+
+    pools = SV.make_scan_pool(maps, seed, n_range[1])
+    mean_p = (p_range[1] - p_range[0]) / math.log(p_range[1] / p_range[0])
+    srv = SV.Server(max_sessions=n_sessions + 64, max_particles=int(min(n_sessions * p_range[1],
+                                                                        n_sessions * mean_p * 4)),
+                    max_points_per_step=(n_sessions + 64) * n_range[1])
+    t0 = time.perf_counter()
+    served = SV.run_load(srv, grids, pools, n_sessions, rate_hz, duration_s, churn_per_s, p_range, n_range, seed=seed)
+    log(f"served {n_sessions} sessions in {time.perf_counter() - t0:.1f}s: {served}")
+    srv.close()
+    plain = SV.run_plain(grids, pools, plain_requests, p_range, n_range, seed=seed)
+    log(f"plain: {plain}")
+    return {
+        "sessions": n_sessions, "rate_hz_per_session": rate_hz, "duration_s": duration_s,
+        "churn_per_s": churn_per_s, "particles": f"log-uniform {p_range}", "points": f"log-uniform {n_range}",
+        "maps": [list(m.dims) for m in maps],
+        "offered_weights_per_s": n_sessions * rate_hz * mean_p * (n_range[1] - n_range[0]) / math.log(
+            n_range[1] / n_range[0]),
+        "weights_per_s": served["weights_per_s"], "p50_ms": served["p50_ms"], "p99_ms": served["p99_ms"],
+        "mean_batch": served["mean_batch"], "requests": served["requests_measured"],
+        "dropped_behind": served["dropped_behind"], "admission_waiting": served["admission_waiting"],
+        "plain_weights_per_s": plain["weights_per_s"], "plain_p50_ms": plain["p50_ms"],
+        "plain_p99_ms": plain["p99_ms"],
+        "served_over_plain": served["weights_per_s"] / plain["weights_per_s"],
+    }
+
+
+def run_served(args, rank, world, local_rank):
+    """Served multi-session localization: sessions spread over four maps
+    (200^3, 400x400x100, 1000x1000x200, 2000x2000x400 cells), Poisson arrivals."""
+    import torch
+
+    import amcl3d_gb300 as A
+    from amcl3d_gb300 import synth as S
+
+    torch.cuda.set_device(local_rank)
+    specs = [((10.0, 10.0, 10.0), 20, 6.0), ((20.0, 20.0, 5.0), 40, None), ((50.0, 50.0, 10.0), 400, 8.0),
+             ((100.0, 100.0, 20.0), 2000, 8.0)]
+    maps, grids = [], []
+    for k, (size, nb, hmax) in enumerate(specs):
+        m = S.make_map(300 + k, size_m=size, n_boxes=nb, max_box_height=hmax)
+        G = A.Grid3d()
+        G.buildGridMap(m.points, m.min, m.max, m.res, S.SENSOR_DEV)
+        m.occ = m.occ if m.dims[0] * m.dims[1] * m.dims[2] < 3e8 else m.occ  # kept for ray casting
+        maps.append(m)
+        grids.append(G)
+    res = served_vs_plain(grids, maps, args.sessions, args.rate, args.duration, args.churn)
+    return {"metric": METRIC + " (served)", "value": res["weights_per_s"], "unit": UNIT, "n_gpus": world,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": {"workload": "served multi-session localization"}, "served": res}
 
 
 def run_reference(args, cfg, rank, world):
@@ -390,13 +456,23 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", choices=sorted(CONFIGS), default="warehouse")
+    ap.add_argument("--config", choices=sorted(CONFIGS) + ["served"], default="warehouse")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sessions", type=int, default=1000, help="served config: concurrent sessions")
+    ap.add_argument("--rate", type=float, default=10.0, help="served config: requests/s per session")
+    ap.add_argument("--duration", type=float, default=20.0, help="served config: measured seconds")
+    ap.add_argument("--churn", type=float, default=5.0, help="served config: sessions joining/leaving per s")
+    ap.add_argument("--served-sessions", type=int, default=200,
+                    help="sessions of the served-vs-plain section of the default line (0: skip)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.config == "served":
+        if rank == 0:
+            print(json.dumps(run_served(args, rank, 1, local_rank)), flush=True)
+        return
     cfg = CONFIGS[args.config]
     if args.impl == "reference":
         res = run_reference(args, cfg, rank, world)

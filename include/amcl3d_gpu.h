@@ -262,6 +262,42 @@ int amcl_batch_autotune(amcl_batch_t b, int reps, int* best_threads, int* best_c
 int amcl_batch_capacity(amcl_batch_t b, uint64_t* free_particles, uint32_t* free_slots);
 int amcl_batch_stream(amcl_batch_t b, void** stream);
 
+/* ---- server: many localisation sessions, continuous batching ------------------------------
+ * No counterpart in the reference.  Sessions are filter slots of an internal batch
+ * (state resident on the device); submitted update requests are served by a scheduler
+ * thread that steps every session with a pending request together, staging requests
+ * that arrive during a step for the next one.  Results come back through
+ * amcl_server_poll in completion order; times are seconds of a monotonic clock. */
+typedef struct amcl_server_s* amcl_server_t;
+typedef struct
+{
+  uint64_t ticket;
+  int64_t session;
+  int32_t status; /* AMCL_OK or the failure of this request's step */
+  int32_t reserved;
+  double t_submit, t_done;
+  float mean[4]; /* x, y, z, yaw after the update */
+  double var[4];
+} amcl_server_result;
+
+int amcl_server_create(amcl_server_t* out, uint32_t max_sessions, uint64_t max_particles, uint64_t max_points_per_step,
+                       void* stream);
+int amcl_server_destroy(amcl_server_t s);
+/* Admission: AMCL_ENOMEM when the session does not fit in the remaining budget.
+ * init8 = (x, y, z, yaw, x_dev, y_dev, z_dev, yaw_dev) of ParticleFilter::init. */
+int amcl_server_open_session(amcl_server_t s, amcl_grid_t grid, uint32_t capacity, uint64_t seed, int num_particles,
+                             const float init8[8], int64_t* session);
+/* Waits for the session's pending requests, then frees its slot. */
+int amcl_server_close_session(amcl_server_t s, int64_t session);
+/* One update request (predict with odom8 unless NULL, update, resample if asked). */
+int amcl_server_submit(amcl_server_t s, int64_t session, const float* xyz, uint32_t n, uint32_t stride_floats,
+                       const float* ranges4, uint32_t nr, const double* odom8, double alpha, double sigma,
+                       double roll, double pitch, int resample, uint64_t* ticket);
+int amcl_server_poll(amcl_server_t s, amcl_server_result* out, uint32_t cap, uint32_t* n);
+int amcl_server_stats(amcl_server_t s, uint64_t* steps, uint64_t* requests, double* busy_s, uint32_t* max_batch,
+                      uint32_t* sessions);
+int amcl_server_batch(amcl_server_t s, amcl_batch_t* batch);
+
 /* Raw stream of the handle (cudaStream_t), for callers that time it with events. */
 int amcl_pf_stream(amcl_pf_t pf, void** stream);
 int amcl_grid_stream(amcl_grid_t g, void** stream);

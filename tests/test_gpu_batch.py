@@ -1,0 +1,127 @@
+"""Batched filters (amcl_batch_*): every filter stepped inside a batch computes exactly
+what the same filter computes stepped alone (same seed, same inputs), whatever the
+other filters in the step; admission against the arena budget; the autotuner keeps
+the filters' state."""
+
+import numpy as np
+import pytest
+
+from amcl3d_gb300 import synth as S
+
+pytestmark = pytest.mark.gpu
+
+MODS = S.ODOM_MODS
+
+
+@pytest.fixture(scope="module")
+def world(amcl):
+    maps = [S.make_map(31, size_m=(8.0, 6.0, 3.0), n_boxes=8), S.make_map(32, size_m=(10.0, 10.0, 4.0), n_boxes=12)]
+    grids = []
+    for m in maps:
+        G = amcl.Grid3d()
+        G.buildGridMap(m.points, m.min, m.max, m.res, S.SENSOR_DEV)
+        grids.append(G)
+    specs = []  # (map index, P, n points, roll, pitch, seed)
+    for k, (mi, P, n, roll, pitch) in enumerate([(0, 300, 400, 0.0, 0.0), (1, 1500, 1000, 0.0, 0.0),
+                                                 (0, 6000, 250, 0.03, -0.02), (1, 20000, 1200, 0.0, 0.0),
+                                                 (0, 700, 0, 0.0, 0.0)]):
+        m = maps[mi]
+        pose = S.free_pose(m, 40 + k, height=1.2, clearance=0.4)
+        scans = [S.ray_cast(m, pose, n_max=n, max_range=8.0, seed=50 + k + 10 * s) if n else
+                 np.zeros((0, 4), np.float32) for s in range(3)]
+        parts = S.particles_around(pose, P, 60 + k)
+        ranges = S.beacons(m, pose, 3, seed=70 + k)
+        specs.append(dict(grid=mi, P=P, scans=scans, parts=parts, ranges=ranges, roll=roll, pitch=pitch,
+                          seed=1000 + k))
+    return grids, specs
+
+
+def run_alone(amcl, grids, sp, steps):
+    pf = amcl.ParticleFilter(seed=sp["seed"])
+    pf.set_particles(sp["parts"])
+    out = []
+    for s in range(steps):
+        pf.predict(*MODS, 0.05, 0.01, 0.0, 0.02)
+        pf.update(grids[sp["grid"]], sp["scans"][s], sp["ranges"], 0.5, 0.1, sp["roll"], sp["pitch"])
+        m = pf.getMean()
+        pf.resample()
+        out.append((pf.particles(), np.array([m.x, m.y, m.z, m.a], np.float32)))
+    return out
+
+
+@pytest.mark.parametrize("tuning", [(256, 1024), (128, 256), (512, 2048)])
+def test_batch_equals_alone(amcl, world, tuning):
+    from amcl3d_gb300.batch import FilterBatch
+
+    grids, specs = world
+    steps = 3
+    alone = [run_alone(amcl, grids, sp, steps) for sp in specs]
+    B = FilterBatch(max_filters=8, max_particles=40000, max_points_per_step=8000)
+    B.set_tuning(*tuning)
+    slots = []
+    for sp in specs:
+        sl = B.add(grids[sp["grid"]], sp["P"], sp["seed"])
+        B.set_particles(sl, sp["parts"])
+        slots.append(sl)
+    odom = (*MODS, 0.05, 0.01, 0.0, 0.02)
+    for s in range(steps):
+        for sl, sp in zip(slots, specs):
+            B.stage(sl, sp["scans"][s], sp["ranges"], odom, 0.5, 0.1, sp["roll"], sp["pitch"], resample=True)
+        B.step()
+        B.wait()
+        for i, (sl, sp) in enumerate(zip(slots, specs)):
+            p_alone, m_alone = alone[i][s]
+            m, _, _ = B.mean_var(sl)
+            np.testing.assert_array_equal(m, m_alone, err_msg=f"filter {i} step {s} mean")
+            np.testing.assert_array_equal(B.particles(sl, sp["P"]), p_alone, err_msg=f"filter {i} step {s}")
+
+
+def test_batch_subset_steps_and_autotune(amcl, world):
+    """Only some filters stage a step; the others keep their state.  The autotuner
+    restores every filter's state."""
+    from amcl3d_gb300.batch import FilterBatch
+
+    grids, specs = world
+    B = FilterBatch(max_filters=8, max_particles=40000, max_points_per_step=8000)
+    slots = [B.add(grids[sp["grid"]], sp["P"], sp["seed"]) for sp in specs]
+    for sl, sp in zip(slots, specs):
+        B.set_particles(sl, sp["parts"])
+    odom = (*MODS, 0.05, 0.01, 0.0, 0.02)
+    B.stage(slots[1], specs[1]["scans"][0], specs[1]["ranges"], odom, 0.5, 0.1)
+    B.stage(slots[3], specs[3]["scans"][0], specs[3]["ranges"], odom, 0.5, 0.1)
+    B.step()
+    B.wait()
+    np.testing.assert_array_equal(B.particles(slots[0], specs[0]["P"]), specs[0]["parts"])
+    before = [B.particles(sl, sp["P"]) for sl, sp in zip(slots, specs)]
+    t, c, ms = B.autotune(reps=2)
+    assert t in (128, 256, 512) and c in (256, 512, 1024, 2048) and ms > 0
+    assert B.tuning() == (t, c)
+    for sl, sp, b in zip(slots, specs, before):
+        np.testing.assert_array_equal(B.particles(sl, sp["P"]), b)
+    alone = run_alone(amcl, grids, specs[3], 2)
+    B.stage(slots[3], specs[3]["scans"][1], specs[3]["ranges"], odom, 0.5, 0.1)
+    B.step()
+    B.wait()
+    np.testing.assert_array_equal(B.particles(slots[3], specs[3]["P"]), alone[1][0])
+
+
+def test_batch_admission(amcl, world):
+    from amcl3d_gb300 import _native as N
+    from amcl3d_gb300.batch import FilterBatch
+
+    grids, _ = world
+    B = FilterBatch(max_filters=2, max_particles=1000, max_points_per_step=100)
+    a = B.add(grids[0], 600, 1)
+    assert B.try_add(grids[0], 2000, 2) is None  # beyond the particle arena
+    b = B.add(grids[0], 256, 3)
+    assert B.try_add(grids[0], 10, 4) is None  # no slot left
+    B.remove(a)
+    c = B.try_add(grids[0], 500, 5)
+    assert c is not None
+    free_p, free_s = B.capacity()
+    assert free_s == 0
+    B.init(b, 200, 1.0, 1.0, 1.0, 0.0, 0.05, 0.05, 0.05, 0.1)
+    big = np.zeros((500, 4), np.float32)
+    B.stage(b, big, None)
+    with pytest.raises(N.AmclError):
+        B.step()  # the staged clouds exceed max_points_per_step
