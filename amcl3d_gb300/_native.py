@@ -122,6 +122,13 @@ _SIGS = {
     "amcl_server_stats": [_vp, C.POINTER(_u64), C.POINTER(_u64), C.POINTER(_d), C.POINTER(_u32), C.POINTER(_u32)],
     "amcl_server_batch": [_vp, C.POINTER(_vp)],
     "amcl_pf_profile": [_vp, _int],
+    "amcl_voxel_create": [C.POINTER(_vp), _vp],
+    "amcl_voxel_destroy": [_vp],
+    "amcl_voxel_stream": [_vp, C.POINTER(_vp)],
+    "amcl_voxel_filter": [_vp, _fp, _u64, _u32, _f, _f, _f, _fp, _u64, C.POINTER(_u64)],
+    "amcl_voxel_filter_dev": [_vp, _vp, _u64, _f, _f, _f, _vp, C.POINTER(_u64)],
+    "amcl_pf_update_voxel": [_vp, _vp, _vp, _fp, _u32, _u32, _f, _f, _f, _fp, _u32, _d, _d, _d, _d, _fp, _u64,
+                             C.POINTER(_u64)],
     "amcl_pf_profile_read": [_vp, _dp, C.POINTER(_u64), _int],
 }
 for _name, _args in _SIGS.items():

@@ -15,6 +15,7 @@
 #include "grid.cuh"
 #include "filter_dev.cuh"
 #include "philox.cuh"
+#include "voxel.cuh"
 
 using namespace amcl;
 
@@ -177,7 +178,10 @@ struct amcl_pf_s
   DevBuf pose[2], w[2], wp[2], wr[2];
   DevBuf inmap, acc, stats, blocksum, hi, ridx, cum, scratch, cloud, ranges, draws, err;
   PinnedBuf h_cloud, h_ranges, h_stats;
+  DevBuf down;          // voxel-downsampled cloud (amcl_pf_update_voxel)
+  PinnedBuf h_down;
   cudaEvent_t staged = nullptr;
+  cudaEvent_t down_ev = nullptr;
   bool staged_pending = false;
   bool blocksum_valid = false;
   bool record = false;
@@ -441,6 +445,8 @@ extern "C" int amcl_pf_destroy(amcl_pf_t pf)
   cudaStreamSynchronize(pf->st.s);
   if (pf->staged)
     cudaEventDestroy(pf->staged);
+  if (pf->down_ev)
+    cudaEventDestroy(pf->down_ev);
   delete pf;
   return AMCL_OK;
 }
@@ -541,6 +547,52 @@ extern "C" int amcl_pf_update_dev(amcl_pf_t pf, amcl_grid_t g, const void* cloud
     return AMCL_OK;
   return pf_update_impl(pf, g, static_cast<const float4*>(cloud_f4_dev), n, ranges4, nr, alpha, sigma, roll, pitch,
                         false);
+}
+
+extern "C" int amcl_pf_update_voxel(amcl_pf_t pf, amcl_grid_t g, amcl_voxel_t v, const float* xyz, uint32_t n,
+                                    uint32_t stride_floats, float leaf_x, float leaf_y, float leaf_z,
+                                    const float* ranges4, uint32_t nr, double alpha, double sigma, double roll,
+                                    double pitch, float* down4, uint64_t down_cap, uint64_t* n_down)
+{
+  PF_GUARD(pf);
+  if (!g || !v || (n && !xyz) || (nr && !ranges4) || stride_floats < 3 || !n_down || (down_cap && !down4))
+    return fail(AMCL_EINVAL, "amcl_pf_update_voxel: bad arguments");
+  const float leaf[3] = { leaf_x, leaf_y, leaf_z };
+  int rc;
+  if ((rc = voxel_check_leaf(leaf, "amcl_pf_update_voxel")))
+    return rc;
+  std::lock_guard<std::mutex> lock_v(v->mu);
+  cudaStream_t s = pf->st.s;
+  if ((rc = stage_host_cloud(pf, xyz, n, stride_floats)) || (rc = pf->down.ensure(std::max<size_t>(n, 1) * 16)))
+    return rc;
+  // Node.cpp:130-137: the voxel filter, on this filter's stream, device to device
+  if ((rc = voxel_enqueue(v, pf->cloud.as<float4>(), n, leaf, pf->down.as<float4>(), s)))
+    return rc;
+  uint32_t m = 0;
+  if (n && (rc = voxel_read_count(v, s, &m)))
+    return rc;
+  *n_down = m;
+  const bool copy_out = down4 && m;
+  if (down4 && m > down_cap)
+    return fail(AMCL_ERANGE, "amcl_pf_update_voxel: down4 holds fewer points than the filter produced");
+  if (copy_out)
+  {
+    if (!pf->down_ev && cudaEventCreateWithFlags(&pf->down_ev, cudaEventDisableTiming) != cudaSuccess)
+      return fail(AMCL_ECUDA, "amcl_pf_update_voxel: cudaEventCreate failed");
+    if ((rc = pf->h_down.ensure(m * 16ull)))
+      return rc;
+    AMCL_CUDA_TRY(cudaMemcpyAsync(pf->h_down.p, pf->down.p, m * 16ull, cudaMemcpyDeviceToHost, s));
+    AMCL_CUDA_TRY(cudaEventRecord(pf->down_ev, s));
+  }
+  // Node.cpp:162: the update weighs the downsampled cloud straight from device memory
+  if (pf->n && (rc = pf_update_impl(pf, g, pf->down.as<float4>(), m, ranges4, nr, alpha, sigma, roll, pitch, false)))
+    return rc;
+  if (copy_out)
+  {
+    AMCL_CUDA_TRY(cudaEventSynchronize(pf->down_ev));
+    std::memcpy(down4, pf->h_down.p, m * 16ull);
+  }
+  return AMCL_OK;
 }
 
 extern "C" int amcl_pf_update_ranges(amcl_pf_t pf, const float* ranges4, uint32_t nr, double alpha, double sigma)

@@ -51,7 +51,7 @@ struct GridView
   uint32_t toff[3];
   float V[3];
   float inv_res[3];
-  float eps[3];  // boundary margin of locate_fast: (size + 2) * 2^-22
+  float eps[3];  // boundary margin of floor_near: (size + 2) * 2^-22
   double min[3];
   uint64_t cells;
   int built;
@@ -123,22 +123,25 @@ __device__ __forceinline__ int locate_pair(float X, const float2* T2, float V, f
   return (X < V) ? k : -1;
 }
 
-// Same result as locate_pair, reading the table only near a cell boundary.
-// q = fl32(X * fl32(1/res)) is within |q| * 2^-23 of X / res, and the reference's
-// floor(fl64(X / res)) differs from floor(X / res) only within 2^-53 relative of an
-// integer; so when frac(q) is at least eps = (size + 2) * 2^-22 away from 0 and 1,
-// floor(q) is the reference's cell.  Otherwise (about 2 eps of the points per axis)
-// the pair table settles it.  X < V and k >= 0 are the reference's bound checks
-// (X < 0 gives k < 0; NaN fails X < V).
-__device__ __forceinline__ int locate_fast(float X, const float2* T2, float V, float inv_res, int size, float eps)
+// Same result as locate_pair for an exact X, reading the table only near a cell
+// boundary.  q = fl32(X * fl32(1/res)) is within |q| * 2^-23 of X / res, and the
+// reference's floor(fl64(X / res)) differs from floor(X / res) only within 2^-53
+// relative of an integer; so when q is at least eps = (size + 2) * 2^-22 away from the
+// nearest integer, floor(q) is the reference's cell.  Otherwise (about 2 eps of the
+// points per axis) the pair table settles it.
+// floor(q) without a float->int conversion: adding 1.5 * 2^23 rounds q to the nearest
+// integer n (the sum lies in [2^23, 2^24), where floats are the integers), read off
+// the sum's bit pattern; d = q - n is exact and floor(q) = n - (d < 0).  This holds for
+// 0 <= q < 2^22; X >= 0 (the reference's lower bound check) keeps q >= 0, X < V keeps
+// q below size + 1, and a size of 2^22 - 2 or more makes eps >= 1, sending every
+// point to the table.  near = |d| < eps.
+__device__ __forceinline__ int floor_near(float X, float inv_res, float eps, bool& near)
 {
   const float q = fmul(X, inv_res);
-  const float fl = floorf(q);
-  const float fr = fsub(q, fl);
-  int k = __float2int_rz(fl);
-  if (fr < eps || fr > 1.0f - eps)
-    k = locate_pair(X, T2, V, inv_res, size);
-  return (X < V && k >= 0) ? k : -1;
+  const float r = fadd(q, 12582912.0f);
+  const float d = fsub(q, fsub(r, 12582912.0f));
+  near = fabsf(d) < eps;
+  return (__float_as_int(r) - 0x4B400000) - (d < 0.0f ? 1 : 0);
 }
 
 // True when a threshold lies within m of X (the estimate may then be on the wrong side).
@@ -207,11 +210,29 @@ __device__ __forceinline__ uint32_t cell_of_point(const GridView& g, const float
   int k[3];
   if (MODE != XF_GENERAL)
   {
+    // X = s + H exactly (float offsets); one branch per point for the rare
+    // near-boundary case, the bound checks of Grid3d.cpp:178-179 folded in.
+    float X[3];
+    bool near = false, valid = true;
 #pragma unroll
     for (int a = 0; a < 3; ++a)
-      k[a] = locate_fast(fadd(s[a], p.H[a]), tab + g.toff[a], g.V[a], g.inv_res[a], static_cast<int>(g.size[a]),
-                         g.eps[a]);
-    return cell_index(g, k[0], k[1], k[2]);
+    {
+      X[a] = fadd(s[a], p.H[a]);
+      bool na;
+      k[a] = floor_near(X[a], g.inv_res[a], g.eps[a], na);
+      near |= na;
+      valid &= (X[a] >= 0.0f) & (X[a] < g.V[a]);  // NaN fails both
+    }
+    if (near)
+    {
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+        k[a] = locate_pair(X[a], tab + g.toff[a], g.V[a], g.inv_res[a], static_cast<int>(g.size[a]));
+      valid = (k[0] | k[1] | k[2]) >= 0;
+    }
+    if (!valid)
+      return 0xFFFFFFFFu;
+    return static_cast<uint32_t>(k[0]) + static_cast<uint32_t>(k[1]) * g.step_y + static_cast<uint32_t>(k[2]) * g.step_z;
   }
   bool amb = false;
 #pragma unroll

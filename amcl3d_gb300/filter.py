@@ -213,6 +213,22 @@ class ParticleFilter:
         N.call("amcl_pf_update", self._h, grid3d.handle, N.fptr(pts), pts.shape[0], stride,
                N.fptr(rg) if rg.size else None, rg.shape[0], float(alpha), float(sigma), float(roll), float(pitch))
 
+    def update_voxel(self, grid3d: Grid3d, voxel: "VoxelGrid", cloud, leaf, range_data, alpha, sigma, roll,
+                     pitch, want_cloud: bool = True):
+        """Node.cpp:130-162 on the device: voxel-downsample the raw scan (pcl::VoxelGrid,
+        leaf = voxel_size) and update with the result without a host round trip.
+        Returns the downsampled cloud ((m, 4) float32; the node publishes it) or its size."""
+        pts, stride = _cloud_array(cloud)
+        rg = _ranges_array(range_data)
+        lf = np.broadcast_to(np.asarray(leaf, dtype=np.float32), (3,))
+        out = np.empty((max(pts.shape[0], 1), 4), np.float32) if want_cloud else None
+        m = C.c_uint64()
+        N.call("amcl_pf_update_voxel", self._h, grid3d.handle, voxel.handle, N.fptr(pts), pts.shape[0], stride,
+               float(lf[0]), float(lf[1]), float(lf[2]), N.fptr(rg) if rg.size else None, rg.shape[0], float(alpha),
+               float(sigma), float(roll), float(pitch), N.fptr(out) if want_cloud else None,
+               out.shape[0] if want_cloud else 0, C.byref(m))
+        return out[: m.value].copy() if want_cloud else int(m.value)
+
     def update_ranges(self, range_data, alpha, sigma) -> None:
         """Range-only update (declared at ParticleFilter.h:157, not defined by the reference)."""
         rg = _ranges_array(range_data)
@@ -284,3 +300,56 @@ class ParticleFilter:
         cnt = (C.c_uint64 * 5)()
         N.call("amcl_pf_profile_read", self._h, ms, cnt, 1 if reset else 0)
         return {name: (ms[i], int(cnt[i])) for i, name in enumerate(N.PROF_NAMES)}
+
+
+class VoxelGrid:
+    """pcl::VoxelGrid<pcl::PointXYZ> as the node uses it (Node.cpp:130-137) on the GPU:
+    ``setInputCloud``, ``setLeafSize``, ``filter``."""
+
+    def __init__(self, stream: int | None = None):
+        self._h = C.c_void_p()
+        N.call("amcl_voxel_create", C.byref(self._h), C.c_void_p(stream) if stream else None)
+        self._cloud = np.zeros((0, 4), np.float32)
+        self._leaf = (1.0, 1.0, 1.0)
+
+    def close(self) -> None:
+        if self._h:
+            N.lib.amcl_voxel_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    def setInputCloud(self, cloud) -> None:
+        self._cloud = _cloud_array(cloud)[0]
+
+    def setLeafSize(self, lx: float, ly: float, lz: float) -> None:
+        self._leaf = (float(lx), float(ly), float(lz))
+
+    def filter(self) -> np.ndarray:
+        return self.downsample(self._cloud, self._leaf)
+
+    def downsample(self, cloud, leaf) -> np.ndarray:
+        """Centroids ((m, 4) float32, w = 1) of the occupied leaves, in voxel-key order."""
+        pts, stride = _cloud_array(cloud)
+        lf = np.broadcast_to(np.asarray(leaf, dtype=np.float32), (3,))
+        out = np.empty((max(pts.shape[0], 1), 4), np.float32)
+        m = C.c_uint64()
+        N.call("amcl_voxel_filter", self._h, N.fptr(pts), pts.shape[0], stride, float(lf[0]), float(lf[1]),
+               float(lf[2]), N.fptr(out), out.shape[0], C.byref(m))
+        return out[: m.value].copy()
+
+    def downsample_dev(self, in_ptr: int, n: int, leaf, out_ptr: int) -> int:
+        """Device float4 buffers (16-byte aligned; out has room for n points); returns the count."""
+        lf = np.broadcast_to(np.asarray(leaf, dtype=np.float32), (3,))
+        m = C.c_uint64()
+        N.call("amcl_voxel_filter_dev", self._h, C.c_void_p(in_ptr), int(n), float(lf[0]), float(lf[1]),
+               float(lf[2]), C.c_void_p(out_ptr), C.byref(m))
+        return int(m.value)

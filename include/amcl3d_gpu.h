@@ -52,6 +52,7 @@ enum
 
 typedef struct amcl_grid_s* amcl_grid_t;
 typedef struct amcl_pf_s* amcl_pf_t;
+typedef struct amcl_voxel_s* amcl_voxel_t;
 
 /* Mirrors PointCloudInfo's bounds/resolution (PointCloudTools.h:54-68) and
  * Grid3dInfo's sizes (PointCloudTools.h:37-50). */
@@ -214,6 +215,38 @@ int amcl_pf_record_draws(amcl_pf_t pf, int enable);
 int amcl_pf_get_draws(amcl_pf_t pf, float* out, uint32_t cap_floats);
 /* Debug/parity: the last resample's source index per output particle. */
 int amcl_pf_get_resample_index(amcl_pf_t pf, int32_t* out, uint32_t cap);
+
+/* ---- scan voxel downsample ---------------------------------------------------------
+ * pcl::VoxelGrid<pcl::PointXYZ> as Node.cpp:130-137 runs it on every accepted scan
+ * (setLeafSize(voxel_size, voxel_size, voxel_size); filter): one centroid per occupied
+ * leaf, in voxel-key order, w component 1; the points of a leaf are summed in input
+ * order; non-finite points are skipped; when the leaf count overflows int32 the input
+ * is returned unchanged.  A handle owns the device scratch and a stream; calls on one
+ * handle are serialised. */
+int amcl_voxel_create(amcl_voxel_t* out, void* stream);
+int amcl_voxel_destroy(amcl_voxel_t v);
+int amcl_voxel_stream(amcl_voxel_t v, void** stream);
+
+/* Host cloud in (n points, stride_floats apart), host centroids out (float4 each, at
+ * most cap); *n_out receives the centroid count (AMCL_ERANGE if it exceeds cap).
+ * Leaf sizes must be positive and finite; n <= 2^30. */
+int amcl_voxel_filter(amcl_voxel_t v, const float* xyz, uint64_t n, uint32_t stride_floats, float leaf_x,
+                      float leaf_y, float leaf_z, float* out4, uint64_t cap, uint64_t* n_out);
+
+/* Device cloud in (n float4, 16-byte aligned), device centroids out (room for n
+ * float4); runs on the handle's stream and synchronises it to return *n_out. */
+int amcl_voxel_filter_dev(amcl_voxel_t v, const void* in_f4_dev, uint64_t n, float leaf_x, float leaf_y, float leaf_z,
+                          void* out_f4_dev, uint64_t* n_out);
+
+/* Node.cpp:130-162 on the device: the raw host scan is copied in once, downsampled
+ * by the voxel filter on this filter's stream and weighed from device memory by
+ * ParticleFilter::update (as amcl_pf_update).  The downsampled cloud (the node
+ * publishes it) is copied to down4 when down4 is not NULL (at most down_cap points,
+ * AMCL_ERANGE beyond); *n_down receives its size. */
+int amcl_pf_update_voxel(amcl_pf_t pf, amcl_grid_t g, amcl_voxel_t v, const float* xyz, uint32_t n,
+                         uint32_t stride_floats, float leaf_x, float leaf_y, float leaf_z, const float* ranges4,
+                         uint32_t nr, double alpha, double sigma, double roll, double pitch, float* down4,
+                         uint64_t down_cap, uint64_t* n_down);
 
 /* ---- batches: many filters stepped together ------------------------------------------------
  * No counterpart in the reference (one filter per node there).  A batch owns fixed

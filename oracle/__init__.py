@@ -59,8 +59,7 @@ class OrcGrid(C.Structure):
 
 
 def _load_oracle():
-    if not _ORC_PATH.exists():
-        subprocess.run(["make", "-s", "-C", str(HERE), "all"], check=True)
+    subprocess.run(["make", "-s", "-C", str(HERE), "all"], check=True)
     lib = C.CDLL(str(_ORC_PATH))
     lib.orc_cloud_weights.argtypes = [C.POINTER(OrcGrid), _fp, C.c_uint64, _fp, C.c_uint64, C.c_uint32, C.c_float,
                                       C.c_float, C.c_int, _fp, _i64p]
@@ -83,6 +82,8 @@ def _load_oracle():
     lib.orc_compute_grid.restype = C.c_int
     lib.orc_philox4x32_10.argtypes = [_u32p, _u32p, _u32p]
     lib.orc_philox4x32_10.restype = None
+    lib.orc_voxel_downsample.argtypes = [_fp, C.c_uint64, C.c_uint32, _fp, _fp, C.POINTER(C.c_uint64)]
+    lib.orc_voxel_downsample.restype = C.c_int
     return lib
 
 
@@ -295,6 +296,19 @@ def compute_grid(points, mn, mx, res, sensor_dev, lo=None, hi=None, exp_mode=1, 
     if rc:
         raise RuntimeError(f"orc_compute_grid failed ({rc})")
     return dist, prob
+
+
+def voxel_downsample(cloud, leaf):
+    """pcl::VoxelGrid<PointXYZ> as called by Node.cpp:130-137 (PCL's published algorithm;
+    a voxel's points summed in input order).  cloud: (n, 3|4) float32; leaf: scalar or 3.
+    Returns (float32 (m, 4) centroids in voxel-key order with w = 1, overflowed flag)."""
+    c = np.ascontiguousarray(cloud, dtype=np.float32)
+    n = c.shape[0]
+    lf = np.broadcast_to(np.asarray(leaf, dtype=np.float32), (3,)).copy()
+    out = np.empty((max(n, 1), 4), np.float32)
+    m = C.c_uint64(0)
+    ovf = orc.orc_voxel_downsample(_f(c), n, c.shape[1] if n else 4, _f(lf), _f(out), C.byref(m))
+    return out[: m.value].copy(), bool(ovf)
 
 
 def philox4x32_10(ctr, key):

@@ -8,6 +8,7 @@
 #define _GNU_SOURCE
 #include "amcl3d_oracle.h"
 
+#include <float.h>
 #include <math.h>
 #include <pthread.h>
 #include <stdlib.h>
@@ -513,4 +514,125 @@ void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t ou
   out[1] = c1;
   out[2] = c2;
   out[3] = c3;
+}
+
+/* ---- scan voxel downsample (pcl::VoxelGrid<PointXYZ>, Node.cpp:130-137) ------------------- */
+
+/* PCL's VoxelGrid is a third-party dependency whose source is not in the reference tree
+ * (package.xml lists pcl_ros without a version; the README targets ROS Kinetic, whose
+ * PCL is 1.7.x).  This restates its published algorithm (VoxelGrid::applyFilter):
+ *   inverse leaf = 1.0f / leaf (float);  min/max over the finite points (float);
+ *   voxel counts d = (int64)((max - min) * inv) + 1 per axis; if dx*dy*dz > INT32_MAX the
+ *     filter warns and returns its input unchanged;
+ *   min_b = (int)floor(min * inv);  div_b = (int)floor(max * inv) - min_b + 1;
+ *   per finite point: ijk = (int)(floor(p * inv) - (float)min_b), key = i + j*div_b.x +
+ *     k*div_b.x*div_b.y;  sort the (key, point) pairs by key;
+ *   per run of equal keys: centroid = first point, += each further point (float), then
+ *     /= (float)count; output points in key order, w component 1.
+ * The reference sorts with std::sort, whose order among equal keys is unspecified; here
+ * the points of a voxel are summed in input order (a stable sort).  With two points per
+ * voxel the order cannot matter (float addition commutes).  Returns 1 when the overflow
+ * rule returned the input, 0 otherwise; *n_out receives the output count (out must hold
+ * n float4 points). */
+static int cmp_u64(const void* a, const void* b)
+{
+  const uint64_t x = *(const uint64_t*)a, y = *(const uint64_t*)b;
+  return (x > y) - (x < y);
+}
+
+int orc_voxel_downsample(const float* xyz, uint64_t n, uint32_t stride, const float leaf[3], float* out4,
+                         uint64_t* n_out)
+{
+  float inv[3], mn[3] = { FLT_MAX, FLT_MAX, FLT_MAX }, mx[3] = { -FLT_MAX, -FLT_MAX, -FLT_MAX };
+  uint64_t n_fin = 0;
+  for (int a = 0; a < 3; ++a)
+    inv[a] = 1.0f / leaf[a];
+  for (uint64_t i = 0; i < n; ++i)
+  {
+    const float* p = xyz + i * stride;
+    if (!(isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2])))
+      continue;
+    ++n_fin;
+    for (int a = 0; a < 3; ++a)
+    {
+      if (p[a] < mn[a])
+        mn[a] = p[a];
+      if (p[a] > mx[a])
+        mx[a] = p[a];
+    }
+  }
+  *n_out = 0;
+  if (n_fin == 0)
+    return 0;
+  /* voxel counts (int64)span + 1 and their product; the product in double, since PCL's
+   * int64 product wraps (undefined) beyond 2^63 and a span of 2^31 or more overflows on
+   * its own.  The key space div_b.x*div_b.y*div_b.z must also fit 32 bits (PCL's int
+   * key would wrap); both count as the overflow that returns the input. */
+  double dprod = 1.0, bprod = 1.0;
+  int32_t min_b[3], div_b[3];
+  for (int a = 0; a < 3; ++a)
+  {
+    const float span = (mx[a] - mn[a]) * inv[a];
+    dprod *= span < 2147483648.0f ? (double)((int64_t)span + 1) : 4294967296.0;
+    const float lo = mn[a] * inv[a], hi = mx[a] * inv[a];
+    min_b[a] = (int32_t)floorf(lo);
+    div_b[a] = (int32_t)floorf(hi) - min_b[a] + 1;
+    bprod *= (double)div_b[a];
+  }
+  if (dprod > (double)INT32_MAX || bprod > 4294967295.0)
+  {
+    for (uint64_t i = 0; i < n; ++i)
+    {
+      const float* p = xyz + i * stride;
+      out4[4 * i + 0] = p[0];
+      out4[4 * i + 1] = p[1];
+      out4[4 * i + 2] = p[2];
+      out4[4 * i + 3] = 1.0f;
+    }
+    *n_out = n;
+    return 1;
+  }
+  const uint32_t mul1 = (uint32_t)div_b[0], mul2 = (uint32_t)div_b[0] * (uint32_t)div_b[1];
+  uint64_t* kv = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)n_fin);
+  uint64_t m = 0;
+  for (uint64_t i = 0; i < n; ++i)
+  {
+    const float* p = xyz + i * stride;
+    if (!(isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2])))
+      continue;
+    uint32_t ijk[3];
+    for (int a = 0; a < 3; ++a)
+    {
+      const float q = p[a] * inv[a];
+      ijk[a] = (uint32_t)(int32_t)(floorf(q) - (float)min_b[a]);
+    }
+    const uint32_t key = ijk[0] + ijk[1] * mul1 + ijk[2] * mul2;
+    kv[m++] = ((uint64_t)key << 32) | (uint64_t)(uint32_t)i;
+  }
+  qsort(kv, (size_t)m, sizeof(uint64_t), cmp_u64);
+  uint64_t v = 0;
+  for (uint64_t j = 0; j < m;)
+  {
+    const uint32_t key = (uint32_t)(kv[j] >> 32);
+    const float* p = xyz + (kv[j] & 0xFFFFFFFFu) * stride;
+    float c[3] = { p[0], p[1], p[2] };
+    uint64_t e = j + 1;
+    for (; e < m && (uint32_t)(kv[e] >> 32) == key; ++e)
+    {
+      const float* q = xyz + (kv[e] & 0xFFFFFFFFu) * stride;
+      c[0] = c[0] + q[0];
+      c[1] = c[1] + q[1];
+      c[2] = c[2] + q[2];
+    }
+    const float cnt = (float)(e - j);
+    out4[4 * v + 0] = c[0] / cnt;
+    out4[4 * v + 1] = c[1] / cnt;
+    out4[4 * v + 2] = c[2] / cnt;
+    out4[4 * v + 3] = 1.0f;
+    ++v;
+    j = e;
+  }
+  free(kv);
+  *n_out = v;
+  return 0;
 }

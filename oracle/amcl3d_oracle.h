@@ -69,6 +69,13 @@ int orc_compute_grid(const float* xyz, uint64_t n, uint32_t stride, const double
                      double res, double sensor_dev, const uint32_t lo[3], const uint32_t hi[3], int exp_mode,
                      int threads, float* dist, float* prob);
 
+/* pcl::VoxelGrid<PointXYZ>::filter (Node.cpp:130-137; PCL's published algorithm, the
+ * points of a voxel summed in input order): out4 (n float4) receives the centroids in
+ * voxel-key order, *n_out their count.  Returns 1 if the voxel count overflowed int32 and
+ * the input was returned unchanged. */
+int orc_voxel_downsample(const float* xyz, uint64_t n, uint32_t stride, const float leaf[3], float* out4,
+                         uint64_t* n_out);
+
 /* Philox4x32-10 block (Salmon et al., SC'11). */
 void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 

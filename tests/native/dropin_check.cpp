@@ -1,6 +1,7 @@
 // Drives the drop-in amcl3d::Grid3d / amcl3d::ParticleFilter the way amcl3d::Node
 // does (Node.cpp:41-53 open + slice + map cloud, :387 init, :154 predict,
-// :162 update, :167 getMean, :181 resample, :104 buildParticlesPoseMsg) and dumps
+// :130-137 voxel filter, :162 update, :167 getMean, :181 resample,
+// :104 buildParticlesPoseMsg) and dumps
 // what the Python test compares with the oracle.
 //
 // usage: dropin_check <map.bt> <scan.f32 (n x 4 floats)> <ranges.f32 (b x 4)> <out dir>
@@ -11,6 +12,7 @@
 #include <vector>
 
 #include "ParticleFilter.h"
+#include "VoxelGrid.h"
 
 using namespace amcl3d;
 
@@ -78,5 +80,18 @@ int main(int argc, char** argv)
   std::vector<Range> none;
   pf.update(none, 0.5, 0.1);  // range-only overload, no ranges: every weight 0
   std::printf("ranges_only_mean %.9g\n", pf.getMean().x);
+
+  // Node.cpp:130-137: the scan filter, with the node's call sequence
+  VoxelGrid sor;
+  sor.setInputCloud(cloud);
+  sor.setLeafSize(0.1f, 0.1f, 0.1f);
+  pcl::PointCloud<pcl::PointXYZ>::Ptr cloud_down(new pcl::PointCloud<pcl::PointXYZ>);
+  sor.filter(*cloud_down);
+  std::printf("voxel %zu %u\n", cloud_down->points.size(), cloud_down->width);
+  {
+    std::ofstream f(out + "/voxel.bin", std::ios::binary);
+    for (const auto& p : cloud_down->points)
+      f.write(reinterpret_cast<const char*>(&p.x), 3 * sizeof(float));
+  }
   return 0;
 }

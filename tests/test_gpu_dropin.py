@@ -64,3 +64,8 @@ def test_dropin_like_the_node(dropin_bin, ref_small, tmp_path):
     w = O.cloud_weights(g, [[2.5, 2.0, 1.2, 0.3]], scan, 0.0, 0.0, yaw_trig=1)[0]
     assert np.float32(float(out["weight"][0])) == w
     assert float(out["ranges_only_mean"][0]) == 0.0
+    # the scan filter the node runs first (Node.cpp:130-137), against the oracle's VoxelGrid
+    down, ovf = O.voxel_downsample(scan, 0.1)
+    assert not ovf and out["voxel"] == [str(down.shape[0])] * 2
+    got = np.fromfile(tmp_path / "voxel.bin", np.float32).reshape(-1, 3)
+    np.testing.assert_array_equal(got, down[:, :3])

@@ -221,3 +221,62 @@ def test_synth_is_deterministic():
     p = S.free_pose(m1, 1)
     np.testing.assert_array_equal(S.ray_cast(m1, p, seed=4, n_max=200), S.ray_cast(m2, p, seed=4, n_max=200))
     assert math.isclose(S.free_pose(m1, 1)[0], p[0])
+
+
+def _voxel_numpy(cloud, leaf):
+    """Second, independent restatement of pcl::VoxelGrid (numpy float32 keys, a stable
+    argsort, per-leaf sums in input order in a Python loop) for the oracle's C version."""
+    c = np.asarray(cloud, np.float32)[:, :3]
+    fin = np.isfinite(c).all(axis=1)
+    p = c[fin]
+    inv = np.float32(1.0) / np.asarray(leaf, np.float32) * np.ones(3, np.float32)
+    mn, mx = p.min(axis=0), p.max(axis=0)
+    span = (mx - mn) * inv
+    d = span.astype(np.int64) + 1
+    if float(d[0]) * float(d[1]) * float(d[2]) > 2**31 - 1:
+        return None
+    min_b = np.floor(mn * inv).astype(np.int64)
+    div_b = np.floor(mx * inv).astype(np.int64) - min_b + 1
+    ijk = (np.floor(p * inv) - min_b.astype(np.float32)).astype(np.int64)
+    key = ijk[:, 0] + ijk[:, 1] * div_b[0] + ijk[:, 2] * div_b[0] * div_b[1]
+    order = np.argsort(key, kind="stable")
+    out = []
+    i = 0
+    while i < order.size:
+        j = i
+        s = p[order[i]].copy()
+        while j + 1 < order.size and key[order[j + 1]] == key[order[i]]:
+            j += 1
+            s = (s + p[order[j]]).astype(np.float32)
+        out.append(np.append(s / np.float32(j - i + 1), np.float32(1.0)))
+        i = j + 1
+    return np.array(out, np.float32).reshape(-1, 4)
+
+
+@pytest.mark.parametrize("leaf", [0.1, 0.5, (0.05, 0.2, 0.3)])
+def test_voxel_oracle_two_restatements(leaf):
+    rng = np.random.default_rng(3)
+    centers = rng.uniform(-4, 4, (150, 3))
+    cloud = (centers[rng.integers(0, 150, 3000)] + rng.normal(0, 0.05, (3000, 3))).astype(np.float32)
+    cloud[rng.integers(0, 3000, 30), 1] = np.nan
+    got, ovf = O.voxel_downsample(cloud, leaf)
+    assert not ovf
+    np.testing.assert_array_equal(got, _voxel_numpy(cloud, leaf))
+
+
+def test_voxel_oracle_properties():
+    """Size-independent properties: one centroid per distinct leaf, all inside the cloud's
+    bounding box, w = 1; the int32 overflow returns the input; empty in, empty out."""
+    rng = np.random.default_rng(4)
+    cloud = rng.uniform(-10, 10, (20000, 4)).astype(np.float32)
+    out, ovf = O.voxel_downsample(cloud, 0.7)
+    inv = np.float32(1.0) / np.float32(0.7)
+    leaves = np.unique(np.floor(cloud[:, :3] * inv), axis=0)
+    assert out.shape[0] == leaves.shape[0] and not ovf
+    assert (out[:, 3] == 1.0).all()
+    assert (out[:, :3] >= cloud[:, :3].min(axis=0)).all() and (out[:, :3] <= cloud[:, :3].max(axis=0)).all()
+    same, ovf = O.voxel_downsample(cloud, 1e-4)
+    assert ovf and same.shape[0] == cloud.shape[0]
+    np.testing.assert_array_equal(same[:, :3], cloud[:, :3])
+    empty, ovf = O.voxel_downsample(np.zeros((0, 4), np.float32), 0.1)
+    assert empty.shape == (0, 4) and not ovf
