@@ -75,6 +75,8 @@ _SIGS = {
     "amcl_grid_is_into_map": [_vp, _f, _f, _f, C.POINTER(_int)],
     "amcl_grid_cloud_weights": [_vp, _fp, _u32, _fp, _u32, _u32, _f, _f, _fp],
     "amcl_grid_cloud_weights_noalloc": [_vp, _vp, _u32, _vp, _u32, _f, _f, _vp, _vp],
+    "amcl_octomap_read": [C.c_char_p, _fp, _u64, C.POINTER(_u64), _dp, _dp, _dp, C.POINTER(_u64)],
+    "amcl_grid_open": [_vp, C.c_char_p, _d, C.POINTER(_u64)],
     "amcl_grid_slice": [_vp, _d, C.POINTER(C.c_int8), _u64, C.POINTER(_u64), C.POINTER(_u32), C.POINTER(_u32)],
     "amcl_grid_stream": [_vp, C.POINTER(_vp)],
     "amcl_pf_create": [C.POINTER(_vp), _u64, _vp],

@@ -66,12 +66,12 @@ def build_gpu(force: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
     LIB.mkdir(exist_ok=True)
     headers = sorted(CSRC.glob("*.cuh")) + [INCLUDE / "amcl3d_gpu.h"]
-    sources = sorted(CSRC.glob("*.cu"))
+    sources = sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))  # .cpp: host-only units
     objs = []
     jobs = []
     nv = nvcc()
     for src in sources:
-        obj = BUILD / (src.stem + ".o")
+        obj = BUILD / (src.name.replace(".", "_") + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
             jobs.append([nv, *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)])

@@ -44,6 +44,20 @@ def _ranges_array(range_data) -> np.ndarray:
     return r
 
 
+def read_octomap(path) -> dict:
+    """openOcTree + computePointCloud (PointCloudTools.cpp:26-82) by the library's
+    octomap reader: {points (n, 4) float32, min, max, res, nodes}; raises AmclError
+    where the reference throws."""
+    n, nodes, res = C.c_uint64(), C.c_uint64(), C.c_double()
+    mn, mx = np.zeros(3), np.zeros(3)
+    N.call("amcl_octomap_read", str(path).encode(), None, 0, C.byref(n), N.dptr(mn), N.dptr(mx), C.byref(res),
+           C.byref(nodes))
+    pts = np.empty((max(n.value, 1), 4), np.float32)
+    N.call("amcl_octomap_read", str(path).encode(), N.fptr(pts), pts.shape[0], C.byref(n), N.dptr(mn), N.dptr(mx),
+           C.byref(res), C.byref(nodes))
+    return {"points": pts[: n.value], "min": tuple(mn), "max": tuple(mx), "res": res.value, "nodes": nodes.value}
+
+
 class Grid3d:
     """amcl3d::Grid3d on the GPU."""
 
@@ -67,6 +81,15 @@ class Grid3d:
         return self._h
 
     # -- map building ------------------------------------------------------------------
+    def open(self, map_path: str, sensor_dev: float) -> bool:
+        """Grid3d::open (Grid3d.cpp:25-78): octomap .bt/.ot -> occupied leaf centres ->
+        the .grid file beside the map, or the GPU distance field (then saved there).
+        False (with the reason in ``last_error``) where the reference logs and returns false."""
+        n = C.c_uint64()
+        rc = N.lib.amcl_grid_open(self._h, str(map_path).encode(), float(sensor_dev), C.byref(n))
+        self.last_error = None if rc == N.AMCL_OK else N.lib.amcl_last_error().decode(errors="replace")
+        return rc == N.AMCL_OK
+
     def buildGridMap(self, points, bounds_min, bounds_max, resolution: float, sensor_dev: float) -> bool:
         """computeGrid (PointCloudTools.cpp:84-149) on the occupied-leaf centres."""
         pts, stride = _cloud_array(points)

@@ -132,6 +132,22 @@ int amcl_grid_cloud_weights(amcl_grid_t g, const float* poses4, uint32_t P, cons
 int amcl_grid_cloud_weights_noalloc(amcl_grid_t g, const void* poses_f4_dev, uint32_t P, const void* cloud_f4_dev,
                                     uint32_t n, float roll, float pitch, float* out_dev, void* stream);
 
+/* openOcTree + computePointCloud (PointCloudTools.cpp:26-82) without the octomap
+ * library, from octomap's file formats (.bt binary, .ot full): the centres of the
+ * occupied leaves as float4 (x, y, z, 1) in the leaf iterator's order (at most cap;
+ * xyz4 may be NULL to ask for the count), the metric bounds over every leaf and the
+ * resolution.  AMCL_EIO when the file cannot be read; AMCL_EINVAL for another
+ * extension, a malformed file, a tree that is not an OcTree or an empty tree (the
+ * cases where openOcTree / computePointCloud throw). */
+int amcl_octomap_read(const char* path, float* xyz4, uint64_t cap, uint64_t* n_points, double min[3], double max[3],
+                      double* resolution, uint64_t* tree_nodes);
+
+/* Grid3d::open (Grid3d.cpp:25-78): reads the map as amcl_octomap_read does, loads
+ * the .grid file beside it when that matches (amcl_grid_load), else builds the
+ * distance field on the GPU and writes that file (a failed write is not an error).
+ * *n_points (may be NULL) receives the occupied leaf count. */
+int amcl_grid_open(amcl_grid_t g, const char* map_path, double sensor_dev, uint64_t* n_points);
+
 /* Grid3d::buildGridSliceMsg (Grid3d.cpp:80-121): int8 occupancy of the z slice,
  * prob scaled to 0..100 by the slice maximum.  Writes min(cap, len) values; *len,
  * *width, *height receive the message sizes.  AMCL_EINVAL when z is outside the map. */
