@@ -111,6 +111,7 @@ _SIGS = {
     "amcl_batch_wait": [_vp],
     "amcl_batch_get_mean": [_vp, _int, _fp, _dp],
     "amcl_batch_set_tuning": [_vp, _int, _int],
+    "amcl_batch_set_split": [_vp, _int, _u64],
     "amcl_batch_get_tuning": [_vp, C.POINTER(_int), C.POINTER(_int)],
     "amcl_batch_autotune": [_vp, _int, C.POINTER(_int), C.POINTER(_int), C.POINTER(_d)],
     "amcl_batch_capacity": [_vp, C.POINTER(_u64), C.POINTER(_u32)],

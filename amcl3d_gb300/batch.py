@@ -92,6 +92,10 @@ class FilterBatch:
         N.call("amcl_batch_get_mean", self._h, int(slot), N.fptr(m), N.dptr(mv))
         return m[:4].copy(), mv[:4].copy(), mv[4:].copy()
 
+    def set_split(self, mode: int, scratch_bytes: int = 0) -> None:
+        """Point-parallel weighting of small steps: 0 auto, 1 never, 2 always."""
+        N.call("amcl_batch_set_split", self._h, int(mode), int(scratch_bytes))
+
     def set_tuning(self, threads: int, chunk: int) -> None:
         N.call("amcl_batch_set_tuning", self._h, int(threads), int(chunk))
 

@@ -16,6 +16,15 @@
 // indices are bit-identical to stepping it alone (the normalisation sums are exact
 // integer sums, independent of how items interleave).
 //
+// Small steps (too few particle tiles to fill the GPU, the served case) split the
+// scan instead: items are (32-particle tile, 256-point slice) pairs spread over every
+// SM, each writing its probabilities to a [tile][point][lane] scratch slab; the block
+// that completes a tile's last slice (a per-tile atomic counter) sums the tile's slab
+// in cloud order while it is still in L2.  The float sums, and so every result, are
+// the same as the fused path's.  The per-particle transforms of a split step are
+// computed once, after predict.  Each step's graph holds only the weighting kernels
+// of the (storage, sum, fused/split) classes it uses.
+//
 // Tuning: the particle tile (threads per block of the weighting kernel) and the point
 // tile (scan points staged in shared memory per iteration) are chosen by
 // amcl_batch_autotune, which times the weighting phase of the staged step under each
@@ -45,7 +54,9 @@ enum : uint32_t
 struct SlotStep
 {
   uint32_t slot, flags, P, N, nr, cur;
+  uint32_t split, tile_base;  // split: point-parallel weighting; first 32-particle tile counter
   uint64_t p_off, c_off;
+  uint64_t sc_off, xf_off;    // split: slab offset (floats), transform record offset
   uint32_t r_off, cloud_sum;
   float sr, cr, sp, cp, k1, k2;
   int yaw_only;
@@ -53,6 +64,13 @@ struct SlotStep
   PredictArgs pred;
   float factor, r;
   GridView g;
+};
+
+// Per-particle transform of a split step (computed once per step).
+struct SplitRec
+{
+  PartXf xf;
+  int inm;
 };
 
 struct BatchDev
@@ -72,7 +90,10 @@ struct BatchDev
   const uint32_t* counts;  // [0] steps, [1] block items, [2] weight items, [4+2c, 5+2c) class c's item range
   const uint2* blk_items;  // (step, local block)
   const uint2* wt_items;   // (step, particle tile)
-  unsigned int* counter;   // weighting work queues, one per class
+  unsigned int* counter;   // weighting work queues: fused classes, then split classes
+  SplitRec* xf;            // split steps' particle transforms
+  float* scratch;          // split steps' probability slabs
+  unsigned int* tile_done; // split: slices finished per 32-particle tile (reset by the last)
 };
 
 constexpr int GRID_BLOCKS_PER_SM = 4;
@@ -120,6 +141,9 @@ __device__ __forceinline__ void b_weigh(const BatchDev& d, const SlotStep& st, u
 // Persistent: blocks take (filter, particle tile) items of one (storage, sum) class
 // until that class's queue is empty.
 constexpr int N_CLASSES = 6;  // 3 storages x 2 sum modes
+// counts: [0] steps, [1] block items, [2] weight items, [4 + 2c, 5 + 2c) fused class
+// c's items, [16 + 2c, 17 + 2c) split class c's items
+constexpr int COUNT_WORDS = 32;
 __host__ __device__ inline int weight_class(int storage, int cloud_sum) { return storage * 2 + (cloud_sum ? 1 : 0); }
 
 template <int STORAGE, int SUM>
@@ -158,6 +182,206 @@ __global__ __launch_bounds__(512) void k_b_weight(BatchDev d, uint32_t chunk, ui
         s_loaded = static_cast<int>(wi.x);
     }
     b_weigh<STORAGE, SUM>(d, st, wi.y, chunk, s_pts, s_rg, s_part, s_tab);
+  }
+}
+
+// Transforms of the particles of split steps (after predict, before the weighting).
+__global__ __launch_bounds__(NT) void k_b_xf(BatchDev d)
+{
+  const uint32_t nitems = d.counts[1];
+  for (uint32_t it = blockIdx.x; it < nitems; it += gridDim.x)
+  {
+    const uint2 bi = d.blk_items[it];
+    const SlotStep& st = d.steps[bi.x];
+    if (!st.split)
+      continue;
+    const uint32_t i = bi.y * NT + threadIdx.x;
+    if (i >= st.P)
+      continue;
+    const float4 pose = d.pose[st.cur][st.p_off + i];
+    SplitRec r;
+    r.xf.exact = 1;
+    r.inm = into_map(st.g, pose.x, pose.y, pose.z) ? 1 : 0;
+    if (r.inm)
+      make_partxf(st.g, st.sr, st.cr, st.sp, st.cp, pose.x, pose.y, pose.z, pose.w, r.xf);
+    d.xf[st.xf_off + i] = r;
+  }
+}
+
+constexpr int SP_WARPS = 8;
+constexpr uint32_t SP_WARP_PTS = 64;                 // points per warp per split item
+constexpr uint32_t SP_PTS = SP_WARPS * SP_WARP_PTS;  // points per split item
+constexpr uint32_t SP_RED_PTS = 64;                  // slab points per reduction stage (8 KB)
+
+__device__ __forceinline__ unsigned int atomic_add_acq_rel_gpu(unsigned int* p, unsigned int v)
+{
+  unsigned int r;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(r) : "l"(p), "r"(v) : "memory");
+  return r;
+}
+
+// Offset (floats) of the reduction buffers in a split block's shared memory.
+__host__ __device__ inline uint32_t split_red_offset(uint32_t tab_cap)
+{
+  const uint32_t bytes = SP_PTS * 16 + MAX_RANGES * 16 + tab_cap * 8;
+  return ((bytes + 15) & ~15u) / 4;
+}
+
+// Persistent: blocks take (split step, tile * slices + slice) items of one class.
+// Each warp covers SP_WARP_PTS points of the slice for the tile's 32 particles.  The
+// block whose count completes the tile streams the tile's slab through shared memory
+// (all warps load, 8 KB per stage, double-buffered; warp 0 adds in cloud order).
+template <int STORAGE, int SUM>
+__global__ __launch_bounds__(SP_WARPS * 32, 3) void k_b_split(BatchDev d, uint32_t tab_cap)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  float4* s_pts = reinterpret_cast<float4*>(smem);
+  float4* s_rg = s_pts + SP_PTS;
+  float2* s_tab = reinterpret_cast<float2*>(s_rg + MAX_RANGES);
+  float* s_red = reinterpret_cast<float*>(smem) + split_red_offset(tab_cap);  // 2 x SP_RED_PTS x 32
+  __shared__ uint32_t s_item;
+  __shared__ int s_loaded;
+  __shared__ int s_last;
+  constexpr int cls = STORAGE * 2 + SUM;
+  const uint32_t begin = d.counts[16 + 2 * cls], end = d.counts[17 + 2 * cls];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (threadIdx.x == 0)
+    s_loaded = -1;
+  while (true)
+  {
+    __syncthreads();
+    if (threadIdx.x == 0)
+      s_item = begin + atomicAdd(d.counter + N_CLASSES + cls, 1u);
+    __syncthreads();
+    const uint32_t it = s_item;
+    if (it >= end)
+      break;
+    const uint2 wi = d.wt_items[it];
+    const SlotStep& st = d.steps[wi.x];
+    const uint32_t nsl = (st.N + SP_PTS - 1) / SP_PTS;
+    const uint32_t tile = wi.y / nsl, slice = wi.y - tile * nsl;
+    const bool load = s_loaded != static_cast<int>(wi.x);  // read by all before thread 0 updates it below
+    if (load)
+    {
+      if (table_entries(st.g) <= tab_cap)
+        load_tables(st.g, s_tab);
+      for (uint32_t i = threadIdx.x; i < st.nr; i += blockDim.x)
+        s_rg[i] = d.ranges[st.r_off + i];
+    }
+    const uint32_t base = slice * SP_PTS;
+    const uint32_t cnt = min(SP_PTS, st.N - base);
+    for (uint32_t i = threadIdx.x; i < SP_PTS; i += blockDim.x)
+    {
+      const float nan = __int_as_float(0x7FC00000);
+      s_pts[i] = i < cnt ? stage_point(d.cloud[st.c_off + base + i], st.yaw_only != 0)
+                         : make_float4(nan, nan, nan, 0.0f);
+    }
+    __syncthreads();
+    if (load && threadIdx.x == 0)
+      s_loaded = static_cast<int>(wi.x);
+    const uint32_t p = tile * 32 + lane;
+    SplitRec rec;
+    rec.inm = 0;
+    rec.xf.exact = 1;
+    if (p < st.P)
+      rec = d.xf[st.xf_off + p];
+    const bool warp_exact = __all_sync(0xFFFFFFFFu, rec.xf.exact != 0);
+    const float* slab = d.scratch + st.sc_off + static_cast<uint64_t>(tile) * st.N * 32;
+    if (rec.inm)
+    {
+      float* out = const_cast<float*>(slab) + lane;
+      const uint32_t k0 = wid * SP_WARP_PTS;
+      if (warp_exact && st.yaw_only)
+        tile_values<STORAGE, XF_YAW>(s_pts, k0, SP_WARP_PTS, cnt, s_tab, st.g, rec.xf, out, base);
+      else if (warp_exact)
+        tile_values<STORAGE, XF_EXACT>(s_pts, k0, SP_WARP_PTS, cnt, s_tab, st.g, rec.xf, out, base);
+      else
+        tile_values<STORAGE, XF_GENERAL>(s_pts, k0, SP_WARP_PTS, cnt, s_tab, st.g, rec.xf, out, base);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+      // Release: the block's slab writes (ordered before by the barrier) are visible
+      // device-wide before the count; acquire: the last block sees every slice's.
+      const unsigned int done = atomic_add_acq_rel_gpu(d.tile_done + st.tile_base + tile, 1u);
+      s_last = done == nsl - 1 ? 1 : 0;
+    }
+    __syncthreads();
+    if (!s_last)
+      continue;
+    // The tile's last slice: sum the slab in cloud order.
+    const float4* slab4 = reinterpret_cast<const float4*>(slab);
+    const uint32_t nst = (st.N + SP_RED_PTS - 1) / SP_RED_PTS;
+    constexpr uint32_t F4_PER_STAGE = SP_RED_PTS * 8;  // 32 floats per point
+    constexpr uint32_t F4_PER_THREAD = F4_PER_STAGE / (SP_WARPS * 32);
+    const uint32_t f4_total = st.N * 8;
+    float4* red4 = reinterpret_cast<float4*>(s_red);
+#pragma unroll
+    for (uint32_t q = 0; q < F4_PER_THREAD; ++q)
+    {
+      const uint32_t f = q * SP_WARPS * 32 + threadIdx.x;
+      if (f < f4_total)
+        red4[f] = __ldcg(slab4 + f);
+    }
+    __syncthreads();
+    CloudSum<SUM> acc;
+    for (uint32_t sg = 0; sg < nst; ++sg)
+    {
+      float4 nxt[F4_PER_THREAD];
+      const uint32_t g0 = (sg + 1) * F4_PER_STAGE;
+#pragma unroll
+      for (uint32_t q = 0; q < F4_PER_THREAD; ++q)
+      {
+        const uint32_t f = g0 + q * SP_WARPS * 32 + threadIdx.x;
+        if (sg + 1 < nst && f < f4_total)
+          nxt[q] = __ldcg(slab4 + f);
+      }
+      if (wid == 0 && rec.inm)
+      {
+        const float* buf = s_red + (sg & 1) * SP_RED_PTS * 32;
+        const uint32_t pts = min(SP_RED_PTS, st.N - sg * SP_RED_PTS);
+        for (uint32_t k = 0; k < pts; ++k)
+        {
+          const float v = buf[k * 32 + lane];
+          if (v >= 0.0f)
+            acc.add(v);
+        }
+      }
+      float4* dst = red4 + ((sg + 1) & 1) * F4_PER_STAGE;
+#pragma unroll
+      for (uint32_t q = 0; q < F4_PER_THREAD; ++q)
+      {
+        const uint32_t f = g0 + q * SP_WARPS * 32 + threadIdx.x;
+        if (sg + 1 < nst && f < f4_total)
+          dst[q * SP_WARPS * 32 + threadIdx.x] = nxt[q];
+      }
+      __syncthreads();
+    }
+    if (wid == 0)
+    {
+      float wpv = 0.0f, wrv = 0.0f;
+      if (rec.inm)
+      {
+        const float4 pose = d.pose[st.cur][st.p_off + p];
+        wpv = acc.weight();
+        wrv = range_weight(pose.x, pose.y, pose.z, s_rg, static_cast<int>(st.nr), st.k1, st.k2);
+        d.wp[st.cur][st.p_off + p] = wpv;
+        d.wr[st.cur][st.p_off + p] = wrv;
+      }
+      if (p < st.P)
+        d.inmap[st.p_off + p] = rec.inm ? 1 : 0;
+      X320 xa = rec.inm ? x320_from_float(wpv) : x320_zero();
+      X320 xb = rec.inm ? x320_from_float(wrv) : x320_zero();
+      xa = x320_warp_sum(xa);
+      xb = x320_warp_sum(xb);
+      if (lane == 0)
+      {
+        unsigned long long* acc_s = d.acc + static_cast<uint64_t>(st.slot) * ACC_WORDS;
+        x320_atomic_add(acc_s + ACC_WP * NDIG, xa);
+        x320_atomic_add(acc_s + ACC_WR * NDIG, xb);
+        d.tile_done[st.tile_base + tile] = 0u;  // ready for the next step
+      }
+    }
   }
 }
 
@@ -273,28 +497,43 @@ struct amcl_batch_s
   std::vector<BatchSlot> slots;
   std::vector<std::pair<uint64_t, uint64_t>> free_ranges;  // particle arena [off, len)
   DevBuf pose[2], w[2], wp[2], wr[2], inmap, hi, blocksum, acc, stats, cloud, ranges, steps, counts, blk_items,
-      wt_items, counter;
+      wt_items, counter, xf, scratch, tile_done;
   PinnedBuf h_cloud, h_ranges, h_steps, h_counts, h_blk, h_wt, h_stats;
   uint32_t n_steps = 0, n_blk = 0, n_wt = 0;
+  uint32_t class_mask = 0;  // weighting classes of the packed step: bits 0-5 fused, 6-11 split
+  int split_mode = 0;       // 0 auto, 1 never, 2 always (when the scratch fits)
+  uint64_t scratch_cap = 4ull << 30;  // bytes of probability slab a split step may use
   uint64_t n_cloud = 0, n_ranges = 0;
   std::vector<uint32_t> step_slots;  // slot of each step in the last launch
   int threads = 256, chunk = 1024;
   uint32_t tab_cap = 0;
-  cudaGraphExec_t exec = nullptr;
-  cudaGraph_t graph = nullptr;
-  int graph_threads = 0, graph_chunk = 0;
-  cudaGraphNode_t n_cloud_cp = nullptr, n_ranges_cp = nullptr, n_steps_cp = nullptr, n_counts_cp = nullptr,
-                  n_blk_cp = nullptr, n_wt_cp = nullptr, n_stats_cp = nullptr;
+  // One instantiated graph per (particle tile, point tile, class mask) in use; all are
+  // dropped when a buffer the kernels point at is reallocated or the tables grow.
+  struct Graph
+  {
+    int threads = 0, chunk = 0;
+    uint32_t mask = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraphNode_t n_cloud_cp = nullptr, n_ranges_cp = nullptr, n_steps_cp = nullptr, n_counts_cp = nullptr,
+                    n_blk_cp = nullptr, n_wt_cp = nullptr;
+  };
+  std::vector<Graph> graphs;
+  void drop_graphs()
+  {
+    for (Graph& g : graphs)
+    {
+      if (g.exec)
+        cudaGraphExecDestroy(g.exec);
+      if (g.graph)
+        cudaGraphDestroy(g.graph);
+    }
+    graphs.clear();
+  }
   bool in_flight = false;
   uint64_t steps_done = 0;
   std::mutex mu;
-  ~amcl_batch_s()
-  {
-    if (exec)
-      cudaGraphExecDestroy(exec);
-    if (graph)
-      cudaGraphDestroy(graph);
-  }
+  ~amcl_batch_s() { drop_graphs(); }
 };
 
 namespace
@@ -323,6 +562,9 @@ BatchDev batch_dev(amcl_batch_s* b)
   d.blk_items = b->blk_items.as<uint2>();
   d.wt_items = b->wt_items.as<uint2>();
   d.counter = b->counter.as<unsigned int>();
+  d.xf = b->xf.as<SplitRec>();
+  d.scratch = b->scratch.as<float>();
+  d.tile_done = b->tile_done.as<unsigned int>();
   return d;
 }
 
@@ -332,41 +574,69 @@ size_t weight_smem(const amcl_batch_s* b, int chunk)
          static_cast<size_t>(b->tab_cap) * sizeof(float2);
 }
 
-// One persistent launch per (storage, sum) class; classes without items exit at once.
-int launch_weight_classes(amcl_batch_s* b, const BatchDev& d, int threads, int chunk, cudaStream_t s)
+size_t split_smem(const amcl_batch_s* b)
+{
+  return static_cast<size_t>(split_red_offset(b->tab_cap)) * 4 + 2ull * SP_RED_PTS * 32 * sizeof(float);
+}
+
+// One persistent launch per weighting class in `mask` (bits 0-5: fused (storage, sum)
+// classes; bits 6-11: the same classes split over points).
+int launch_weight_classes(amcl_batch_s* b, const BatchDev& d, int threads, int chunk, cudaStream_t s, uint32_t mask)
 {
   const unsigned grid = static_cast<unsigned>(device_sm_count() * 2);
-  const size_t smem = weight_smem(b, chunk);
+  const unsigned sgrid = static_cast<unsigned>(device_sm_count() * 3);
+  const size_t smem = weight_smem(b, chunk), ssmem = split_smem(b);
   const uint32_t c = static_cast<uint32_t>(chunk);
-  k_b_weight<AMCL_GRID_F32, 0><<<grid, threads, smem, s>>>(d, c, b->tab_cap);
-  k_b_weight<AMCL_GRID_F32, 1><<<grid, threads, smem, s>>>(d, c, b->tab_cap);
-  k_b_weight<AMCL_GRID_F16, 0><<<grid, threads, smem, s>>>(d, c, b->tab_cap);
-  k_b_weight<AMCL_GRID_F16, 1><<<grid, threads, smem, s>>>(d, c, b->tab_cap);
-  k_b_weight<AMCL_GRID_U8, 0><<<grid, threads, smem, s>>>(d, c, b->tab_cap);
-  k_b_weight<AMCL_GRID_U8, 1><<<grid, threads, smem, s>>>(d, c, b->tab_cap);
+  if (mask & (1u << 0))
+    k_b_weight<AMCL_GRID_F32, 0><<<grid, threads, smem, s>>>(d, c, b->tab_cap);
+  if (mask & (1u << 1))
+    k_b_weight<AMCL_GRID_F32, 1><<<grid, threads, smem, s>>>(d, c, b->tab_cap);
+  if (mask & (1u << 2))
+    k_b_weight<AMCL_GRID_F16, 0><<<grid, threads, smem, s>>>(d, c, b->tab_cap);
+  if (mask & (1u << 3))
+    k_b_weight<AMCL_GRID_F16, 1><<<grid, threads, smem, s>>>(d, c, b->tab_cap);
+  if (mask & (1u << 4))
+    k_b_weight<AMCL_GRID_U8, 0><<<grid, threads, smem, s>>>(d, c, b->tab_cap);
+  if (mask & (1u << 5))
+    k_b_weight<AMCL_GRID_U8, 1><<<grid, threads, smem, s>>>(d, c, b->tab_cap);
+  if (mask & (1u << 6))
+    k_b_split<AMCL_GRID_F32, 0><<<sgrid, SP_WARPS * 32, ssmem, s>>>(d, b->tab_cap);
+  if (mask & (1u << 7))
+    k_b_split<AMCL_GRID_F32, 1><<<sgrid, SP_WARPS * 32, ssmem, s>>>(d, b->tab_cap);
+  if (mask & (1u << 8))
+    k_b_split<AMCL_GRID_F16, 0><<<sgrid, SP_WARPS * 32, ssmem, s>>>(d, b->tab_cap);
+  if (mask & (1u << 9))
+    k_b_split<AMCL_GRID_F16, 1><<<sgrid, SP_WARPS * 32, ssmem, s>>>(d, b->tab_cap);
+  if (mask & (1u << 10))
+    k_b_split<AMCL_GRID_U8, 0><<<sgrid, SP_WARPS * 32, ssmem, s>>>(d, b->tab_cap);
+  if (mask & (1u << 11))
+    k_b_split<AMCL_GRID_U8, 1><<<sgrid, SP_WARPS * 32, ssmem, s>>>(d, b->tab_cap);
   AMCL_LAUNCH_CHECK("k_b_weight");
   return AMCL_OK;
 }
 
-int set_weight_smem(size_t smem)
+template <typename K>
+int smem_attr(K kernel, size_t smem)
 {
-  AMCL_CUDA_TRY(cudaFuncSetAttribute(k_b_weight<AMCL_GRID_F32, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     static_cast<int>(smem)));
-  AMCL_CUDA_TRY(cudaFuncSetAttribute(k_b_weight<AMCL_GRID_F32, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     static_cast<int>(smem)));
-  AMCL_CUDA_TRY(cudaFuncSetAttribute(k_b_weight<AMCL_GRID_F16, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     static_cast<int>(smem)));
-  AMCL_CUDA_TRY(cudaFuncSetAttribute(k_b_weight<AMCL_GRID_F16, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     static_cast<int>(smem)));
-  AMCL_CUDA_TRY(cudaFuncSetAttribute(k_b_weight<AMCL_GRID_U8, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     static_cast<int>(smem)));
-  AMCL_CUDA_TRY(cudaFuncSetAttribute(k_b_weight<AMCL_GRID_U8, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     static_cast<int>(smem)));
+  AMCL_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  return AMCL_OK;
+}
+
+int set_weight_smem(size_t smem, size_t ssmem)
+{
+  int rc;
+  if ((rc = smem_attr(k_b_weight<AMCL_GRID_F32, 0>, smem)) || (rc = smem_attr(k_b_weight<AMCL_GRID_F32, 1>, smem)) ||
+      (rc = smem_attr(k_b_weight<AMCL_GRID_F16, 0>, smem)) || (rc = smem_attr(k_b_weight<AMCL_GRID_F16, 1>, smem)) ||
+      (rc = smem_attr(k_b_weight<AMCL_GRID_U8, 0>, smem)) || (rc = smem_attr(k_b_weight<AMCL_GRID_U8, 1>, smem)) ||
+      (rc = smem_attr(k_b_split<AMCL_GRID_F32, 0>, ssmem)) || (rc = smem_attr(k_b_split<AMCL_GRID_F32, 1>, ssmem)) ||
+      (rc = smem_attr(k_b_split<AMCL_GRID_F16, 0>, ssmem)) || (rc = smem_attr(k_b_split<AMCL_GRID_F16, 1>, ssmem)) ||
+      (rc = smem_attr(k_b_split<AMCL_GRID_U8, 0>, ssmem)) || (rc = smem_attr(k_b_split<AMCL_GRID_U8, 1>, ssmem)))
+    return rc;
   return AMCL_OK;
 }
 
 // Enqueues the whole step on the batch stream (also what the graph captures).
-int enqueue_step(amcl_batch_s* b, int threads, int chunk, bool copies)
+int enqueue_step(amcl_batch_s* b, int threads, int chunk, bool copies, uint32_t mask)
 {
   cudaStream_t s = b->st.s;
   BatchDev d = batch_dev(b);
@@ -374,7 +644,7 @@ int enqueue_step(amcl_batch_s* b, int threads, int chunk, bool copies)
   const unsigned grid = static_cast<unsigned>(sms * GRID_BLOCKS_PER_SM);
   if (copies)
   {
-    AMCL_CUDA_TRY(cudaMemcpyAsync(b->counts.p, b->h_counts.p, 16 * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    AMCL_CUDA_TRY(cudaMemcpyAsync(b->counts.p, b->h_counts.p, COUNT_WORDS * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
     AMCL_CUDA_TRY(cudaMemcpyAsync(b->steps.p, b->h_steps.p, std::max<uint64_t>(b->n_steps, 1) * sizeof(SlotStep),
                                   cudaMemcpyHostToDevice, s));
     AMCL_CUDA_TRY(cudaMemcpyAsync(b->blk_items.p, b->h_blk.p, std::max<uint64_t>(b->n_blk, 1) * sizeof(uint2),
@@ -388,9 +658,14 @@ int enqueue_step(amcl_batch_s* b, int threads, int chunk, bool copies)
   }
   k_b_predict<<<grid, NT, 0, s>>>(d);
   AMCL_LAUNCH_CHECK("k_b_predict");
+  if (mask >> N_CLASSES)
+  {
+    k_b_xf<<<grid, NT, 0, s>>>(d);
+    AMCL_LAUNCH_CHECK("k_b_xf");
+  }
   AMCL_CUDA_TRY(cudaMemsetAsync(b->acc.p, 0, static_cast<size_t>(b->max_filters) * ACC_WORDS * 8, s));
-  AMCL_CUDA_TRY(cudaMemsetAsync(b->counter.p, 0, N_CLASSES * sizeof(unsigned int), s));
-  int rc = launch_weight_classes(b, d, threads, chunk, s);
+  AMCL_CUDA_TRY(cudaMemsetAsync(b->counter.p, 0, 2 * N_CLASSES * sizeof(unsigned int), s));
+  int rc = launch_weight_classes(b, d, threads, chunk, s, mask);
   if (rc)
     return rc;
   k_b_blend<<<grid, NT, 0, s>>>(d);
@@ -409,44 +684,111 @@ int enqueue_step(amcl_batch_s* b, int threads, int chunk, bool copies)
   return AMCL_OK;
 }
 
-// Weighting work items of the packed steps: (step, particle tile of `threads`),
-// grouped by (storage, sum) class, longest scans first within a class (stable, so a
-// filter's tiles stay adjacent and reuse the staged tables); class c's range goes to
-// counts[4 + 2c], counts[5 + 2c].
+// Weighting work items of the packed steps.  Fused steps: (step, particle tile of
+// `threads`), grouped by (storage, sum) class, longest scans first within a class
+// (stable, so a filter's tiles stay adjacent and reuse the staged tables).  Split
+// steps: (step, 32-particle tile * slices + 512-point slice), tile-major so a tile's
+// slices run together and its slab is summed while still in L2.  Sets the class mask.
 void build_weight_items(amcl_batch_s* b, int threads)
 {
   const SlotStep* hs = b->h_steps.as<SlotStep>();
-  struct Item
-  {
-    int cls;
-    uint32_t cost;
-    uint2 it;
-  };
-  std::vector<Item> wt;
-  for (uint32_t s = 0; s < b->n_steps; ++s)
-  {
+  auto step_class = [&](uint32_t s) {
     const int cls = weight_class(hs[s].g.storage, static_cast<int>(hs[s].cloud_sum));
-    const uint32_t ntile = ceil_div(hs[s].P, threads);
-    for (uint32_t k = 0; k < ntile; ++k)
-      wt.push_back({ cls, std::max<uint32_t>(hs[s].N, 1), make_uint2(s, k) });
-  }
-  std::stable_sort(wt.begin(), wt.end(), [](const Item& x, const Item& y) {
-    return x.cls != y.cls ? x.cls < y.cls : x.cost > y.cost;
+    return hs[s].split ? N_CLASSES + cls : cls;
+  };
+  // Steps ordered by class, longest scan first (stable): the items follow step by step.
+  std::vector<uint32_t> order(b->n_steps);
+  for (uint32_t s = 0; s < b->n_steps; ++s)
+    order[s] = s;
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
+    const int cx = step_class(x), cy = step_class(y);
+    return cx != cy ? cx < cy : std::max<uint32_t>(hs[x].N, 1) > std::max<uint32_t>(hs[y].N, 1);
   });
   uint2* hw = b->h_wt.as<uint2>();
   uint32_t* hcnt = b->h_counts.as<uint32_t>();
   for (int c = 0; c < N_CLASSES; ++c)
-    hcnt[4 + 2 * c] = hcnt[5 + 2 * c] = 0;
-  for (size_t k = 0; k < wt.size(); ++k)
+    hcnt[4 + 2 * c] = hcnt[5 + 2 * c] = hcnt[16 + 2 * c] = hcnt[17 + 2 * c] = 0;
+  uint32_t mask = 0, k = 0;
+  int prev = -1;
+  for (uint32_t s : order)
   {
-    hw[k] = wt[k].it;
-    const int c = wt[k].cls;
-    if (k == 0 || wt[k - 1].cls != c)
-      hcnt[4 + 2 * c] = static_cast<uint32_t>(k);
-    hcnt[5 + 2 * c] = static_cast<uint32_t>(k + 1);
+    const int c = step_class(s);
+    const int w = c < N_CLASSES ? 4 + 2 * c : 16 + 2 * (c - N_CLASSES);
+    const uint32_t n = hs[s].split ? ceil_div(hs[s].P, 32) * ceil_div(hs[s].N, SP_PTS) : ceil_div(hs[s].P, threads);
+    if (c != prev)
+      hcnt[w] = k;
+    prev = c;
+    for (uint32_t j = 0; j < n; ++j)
+      hw[k++] = make_uint2(s, j);
+    hcnt[w + 1] = k;
+    if (n)
+      mask |= 1u << c;
   }
-  b->n_wt = static_cast<uint32_t>(wt.size());
+  b->n_wt = k;
+  b->class_mask = mask;
   hcnt[2] = b->n_wt;
+}
+
+// Weighting item capacity the packed steps need (fused and split).
+uint64_t weight_items_needed(const amcl_batch_s* b, int threads)
+{
+  const SlotStep* hs = b->h_steps.as<SlotStep>();
+  uint64_t n = 0;
+  for (uint32_t s = 0; s < b->n_steps; ++s)
+    n += hs[s].split ? static_cast<uint64_t>(ceil_div(hs[s].P, 32)) * ceil_div(hs[s].N, SP_PTS)
+                     : ceil_div(hs[s].P, threads);
+  return n;
+}
+
+// Split decision for the packed steps: point-parallel weighting (all steps with
+// points) when the fused tiles cannot fill the GPU and the slabs fit the scratch
+// budget; assigns the tile counters, slab and transform offsets and sizes the buffers
+// (their reallocation drops the captured graphs).
+constexpr uint32_t SPLIT_BELOW_TILES_PER_SM = 2;
+
+int plan_split(amcl_batch_s* b, int threads)
+{
+  SlotStep* hs = b->h_steps.as<SlotStep>();
+  uint64_t fused_tiles = 0, slab = 0;
+  for (uint32_t s = 0; s < b->n_steps; ++s)
+  {
+    hs[s].split = 0;
+    if (!hs[s].N)
+      continue;
+    fused_tiles += ceil_div(hs[s].P, threads);
+    slab += static_cast<uint64_t>(ceil_div(hs[s].P, 32)) * 32ull * hs[s].N;
+  }
+  bool split = b->split_mode == 2 ||
+               (b->split_mode == 0 && fused_tiles < SPLIT_BELOW_TILES_PER_SM * static_cast<uint64_t>(device_sm_count()));
+  if (!fused_tiles || slab * 4 > b->scratch_cap)
+    split = false;
+  if (!split)
+    return AMCL_OK;
+  uint64_t tiles = 0, sc = 0, xo = 0;
+  for (uint32_t s = 0; s < b->n_steps; ++s)
+  {
+    SlotStep& st = hs[s];
+    if (!st.N)
+      continue;
+    st.split = 1;
+    st.tile_base = static_cast<uint32_t>(tiles);
+    st.sc_off = sc;
+    st.xf_off = xo;
+    tiles += ceil_div(st.P, 32);
+    sc += static_cast<uint64_t>(ceil_div(st.P, 32)) * 32ull * st.N;
+    xo += st.P;
+  }
+  const void* old[3] = { b->xf.p, b->scratch.p, b->tile_done.p };
+  const size_t old_tiles = b->tile_done.bytes;
+  int rc;
+  if ((rc = b->xf.ensure(xo * sizeof(SplitRec))) || (rc = b->scratch.ensure(sc * 4)) ||
+      (rc = b->tile_done.ensure(tiles * 4)))
+    return rc;
+  if (b->tile_done.bytes != old_tiles || b->tile_done.p != old[2])
+    AMCL_CUDA_TRY(cudaMemsetAsync(b->tile_done.p, 0, b->tile_done.bytes, b->st.s));
+  if (b->xf.p != old[0] || b->scratch.p != old[1] || b->tile_done.p != old[2])
+    b->drop_graphs();
+  return AMCL_OK;
 }
 
 // Packs the staged steps of every slot into the pinned staging buffers.
@@ -549,15 +891,23 @@ int pack_steps(amcl_batch_s* b)
   hcnt[0] = ns;
   hcnt[1] = nb;
   hcnt[3] = 0;
+  int rc;
+  if ((rc = plan_split(b, threads)))
+    return rc;
+  const uint64_t items = weight_items_needed(b, threads);
+  if (items * sizeof(uint2) > b->wt_items.bytes)
+  {
+    b->drop_graphs();
+    if ((rc = b->wt_items.ensure(items * sizeof(uint2))) || (rc = b->h_wt.ensure(items * sizeof(uint2))))
+      return rc;
+  }
   build_weight_items(b, threads);
   return AMCL_OK;
 }
 
-int graph_update_copies(amcl_batch_s* b)
+int graph_update_copies(amcl_batch_s* b, amcl_batch_s::Graph& G)
 {
-  // The copies in the graph move the full staging capacity only up to what is used.
-  cudaStream_t s = b->st.s;
-  (void)s;
+  // The copies in the graph move only what the packed step uses.
   struct Cp
   {
     cudaGraphNode_t node;
@@ -566,32 +916,23 @@ int graph_update_copies(amcl_batch_s* b)
     size_t bytes;
   };
   const Cp cps[] = {
-    { b->n_steps_cp, b->steps.p, b->h_steps.p, std::max<uint64_t>(b->n_steps, 1) * sizeof(SlotStep) },
-    { b->n_blk_cp, b->blk_items.p, b->h_blk.p, std::max<uint64_t>(b->n_blk, 1) * sizeof(uint2) },
-    { b->n_wt_cp, b->wt_items.p, b->h_wt.p, std::max<uint64_t>(b->n_wt, 1) * sizeof(uint2) },
-    { b->n_cloud_cp, b->cloud.p, b->h_cloud.p, std::max<uint64_t>(b->n_cloud, 1) * sizeof(float4) },
-    { b->n_ranges_cp, b->ranges.p, b->h_ranges.p, std::max<uint64_t>(b->n_ranges, 1) * sizeof(float4) },
+    { G.n_steps_cp, b->steps.p, b->h_steps.p, std::max<uint64_t>(b->n_steps, 1) * sizeof(SlotStep) },
+    { G.n_blk_cp, b->blk_items.p, b->h_blk.p, std::max<uint64_t>(b->n_blk, 1) * sizeof(uint2) },
+    { G.n_wt_cp, b->wt_items.p, b->h_wt.p, std::max<uint64_t>(b->n_wt, 1) * sizeof(uint2) },
+    { G.n_cloud_cp, b->cloud.p, b->h_cloud.p, std::max<uint64_t>(b->n_cloud, 1) * sizeof(float4) },
+    { G.n_ranges_cp, b->ranges.p, b->h_ranges.p, std::max<uint64_t>(b->n_ranges, 1) * sizeof(float4) },
   };
   for (const Cp& c : cps)
-    AMCL_CUDA_TRY(cudaGraphExecMemcpyNodeSetParams1D(b->exec, c.node, c.dst, c.src, c.bytes, cudaMemcpyHostToDevice));
+    AMCL_CUDA_TRY(cudaGraphExecMemcpyNodeSetParams1D(G.exec, c.node, c.dst, c.src, c.bytes, cudaMemcpyHostToDevice));
   return AMCL_OK;
 }
 
-int build_graph(amcl_batch_s* b)
+// Captures and instantiates the step for the current shape and class mask.
+int build_graph(amcl_batch_s* b, uint32_t mask, amcl_batch_s::Graph& G)
 {
-  if (b->exec)
-  {
-    cudaGraphExecDestroy(b->exec);
-    b->exec = nullptr;
-  }
-  if (b->graph)
-  {
-    cudaGraphDestroy(b->graph);
-    b->graph = nullptr;
-  }
   cudaStream_t s = b->st.s;
   AMCL_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-  int rc = enqueue_step(b, b->threads, b->chunk, true);
+  int rc = enqueue_step(b, b->threads, b->chunk, true, mask);
   cudaGraph_t g = nullptr;
   const cudaError_t e = cudaStreamEndCapture(s, &g);
   if (rc)
@@ -602,7 +943,10 @@ int build_graph(amcl_batch_s* b)
   }
   if (e != cudaSuccess)
     return fail(AMCL_ECUDA, std::string("batch graph capture: ") + cudaGetErrorString(e));
-  b->graph = g;
+  G.graph = g;
+  G.threads = b->threads;
+  G.chunk = b->chunk;
+  G.mask = mask;
   // Find the memcpy nodes by their destinations.
   size_t nn = 0;
   AMCL_CUDA_TRY(cudaGraphGetNodes(g, nullptr, &nn));
@@ -618,21 +962,19 @@ int build_graph(amcl_batch_s* b)
     AMCL_CUDA_TRY(cudaGraphMemcpyNodeGetParams(n, &p));
     const void* dst = p.dstPtr.ptr;
     if (dst == b->steps.p)
-      b->n_steps_cp = n;
+      G.n_steps_cp = n;
     else if (dst == b->blk_items.p)
-      b->n_blk_cp = n;
+      G.n_blk_cp = n;
     else if (dst == b->wt_items.p)
-      b->n_wt_cp = n;
+      G.n_wt_cp = n;
     else if (dst == b->cloud.p)
-      b->n_cloud_cp = n;
+      G.n_cloud_cp = n;
     else if (dst == b->ranges.p)
-      b->n_ranges_cp = n;
+      G.n_ranges_cp = n;
   }
-  if (!b->n_steps_cp || !b->n_blk_cp || !b->n_wt_cp || !b->n_cloud_cp || !b->n_ranges_cp)
+  if (!G.n_steps_cp || !G.n_blk_cp || !G.n_wt_cp || !G.n_cloud_cp || !G.n_ranges_cp)
     return fail(AMCL_ECUDA, "batch graph: copy nodes not found");
-  AMCL_CUDA_TRY(cudaGraphInstantiate(&b->exec, g, 0));
-  b->graph_threads = b->threads;
-  b->graph_chunk = b->chunk;
+  AMCL_CUDA_TRY(cudaGraphInstantiate(&G.exec, g, 0));
   return AMCL_OK;
 }
 
@@ -730,11 +1072,11 @@ extern "C" int amcl_batch_create(amcl_batch_t* out, uint32_t max_filters, uint64
         (rc = b->stats.ensure(static_cast<size_t>(max_filters) * sizeof(PFStats))) ||
         (rc = b->cloud.ensure(pts * 16)) || (rc = b->ranges.ensure(rng * 16)) ||
         (rc = b->steps.ensure(static_cast<size_t>(max_filters) * sizeof(SlotStep))) ||
-        (rc = b->counts.ensure(64)) || (rc = b->blk_items.ensure((cap / NT + max_filters) * sizeof(uint2))) ||
+        (rc = b->counts.ensure(COUNT_WORDS * 4)) || (rc = b->blk_items.ensure((cap / NT + max_filters) * sizeof(uint2))) ||
         (rc = b->wt_items.ensure(items * sizeof(uint2))) || (rc = b->counter.ensure(64)) ||
         (rc = b->h_cloud.ensure(pts * 16)) || (rc = b->h_ranges.ensure(rng * 16)) ||
         (rc = b->h_steps.ensure(static_cast<size_t>(max_filters) * sizeof(SlotStep))) ||
-        (rc = b->h_counts.ensure(64)) || (rc = b->h_blk.ensure((cap / NT + max_filters) * sizeof(uint2))) ||
+        (rc = b->h_counts.ensure(COUNT_WORDS * 4)) || (rc = b->h_blk.ensure((cap / NT + max_filters) * sizeof(uint2))) ||
         (rc = b->h_wt.ensure(items * sizeof(uint2))) ||
         (rc = b->h_stats.ensure(static_cast<size_t>(max_filters) * sizeof(PFStats)));
   if (!rc && cudaMemsetAsync(b->stats.p, 0, static_cast<size_t>(max_filters) * sizeof(PFStats), b->st.s) != cudaSuccess)
@@ -1000,20 +1342,38 @@ extern "C" int amcl_batch_step(amcl_batch_t b)
     return rc;
   if (!b->n_steps)
     return AMCL_OK;
-  if (tab > b->tab_cap || !b->exec || b->graph_threads != b->threads || b->graph_chunk != b->chunk)
+  if (tab > b->tab_cap)
   {
-    b->tab_cap = std::max(tab, b->tab_cap);
-    const size_t smem = weight_smem(b, b->chunk);
-    if (smem > 227 * 1024)
-      return fail(AMCL_ERANGE, "amcl_batch_step: grid tables and point tile exceed shared memory");
-    if ((rc = set_weight_smem(smem)))
-      return rc;
-    if ((rc = build_graph(b)))
-      return rc;
+    b->tab_cap = tab;
+    b->drop_graphs();
   }
-  if ((rc = graph_update_copies(b)))
+  const uint32_t mask = b->class_mask;
+  amcl_batch_s::Graph* G = nullptr;
+  for (auto& g : b->graphs)
+    if (g.threads == b->threads && g.chunk == b->chunk && g.mask == mask)
+      G = &g;
+  if (!G)
+  {
+    const size_t smem = weight_smem(b, b->chunk), ssmem = split_smem(b);
+    if (smem > 227 * 1024 || ssmem > 227 * 1024)
+      return fail(AMCL_ERANGE, "amcl_batch_step: grid tables and point tile exceed shared memory");
+    if ((rc = set_weight_smem(smem, ssmem)))
+      return rc;
+    amcl_batch_s::Graph fresh;
+    if ((rc = build_graph(b, mask, fresh)))
+    {
+      if (fresh.exec)
+        cudaGraphExecDestroy(fresh.exec);
+      if (fresh.graph)
+        cudaGraphDestroy(fresh.graph);
+      return rc;
+    }
+    b->graphs.push_back(fresh);
+    G = &b->graphs.back();
+  }
+  if ((rc = graph_update_copies(b, *G)))
     return rc;
-  AMCL_CUDA_TRY(cudaGraphLaunch(b->exec, b->st.s));
+  AMCL_CUDA_TRY(cudaGraphLaunch(G->exec, b->st.s));
   for (uint32_t si : b->step_slots)
   {
     BatchSlot& sl = b->slots[si];
@@ -1023,7 +1383,8 @@ extern "C" int amcl_batch_step(amcl_batch_t b)
   }
   b->in_flight = true;
   b->steps_done += 1;
-  for (int k = 0; k < 7; ++k)  // the graph's kernels
+  const int kernels = 6 + (mask >> N_CLASSES ? 1 : 0) + __builtin_popcount(mask);  // the graph's kernels
+  for (int k = 0; k < kernels; ++k)
     count_launch();
   return AMCL_OK;
 }
@@ -1064,6 +1425,17 @@ extern "C" int amcl_batch_set_tuning(amcl_batch_t b, int threads, int chunk)
   std::lock_guard<std::mutex> lock(b->mu);
   b->threads = threads;
   b->chunk = chunk;
+  return AMCL_OK;
+}
+
+extern "C" int amcl_batch_set_split(amcl_batch_t b, int mode, uint64_t scratch_bytes)
+{
+  if (!b || mode < 0 || mode > 2)
+    return fail(AMCL_EINVAL, "amcl_batch_set_split: mode 0 (auto), 1 (never) or 2 (always)");
+  std::lock_guard<std::mutex> lock(b->mu);
+  b->split_mode = mode;
+  if (scratch_bytes)
+    b->scratch_cap = scratch_bytes;
   return AMCL_OK;
 }
 
@@ -1145,21 +1517,21 @@ extern "C" int amcl_batch_autotune(amcl_batch_t b, int reps, int* best_threads, 
     build_weight_items(b, t);
     AMCL_CUDA_TRY(cudaMemcpyAsync(b->wt_items.p, b->h_wt.p, std::max<uint64_t>(b->n_wt, 1) * sizeof(uint2),
                                   cudaMemcpyHostToDevice, s));
-    AMCL_CUDA_TRY(cudaMemcpyAsync(b->counts.p, b->h_counts.p, 64, cudaMemcpyHostToDevice, s));
+    AMCL_CUDA_TRY(cudaMemcpyAsync(b->counts.p, b->h_counts.p, COUNT_WORDS * 4, cudaMemcpyHostToDevice, s));
     for (int c : cand_c)
     {
       const size_t smem = weight_smem(b, c);
       if (smem > 227 * 1024)
         continue;
-      if ((rc = set_weight_smem(smem)))
+      if ((rc = set_weight_smem(smem, split_smem(b))))
         return rc;
       float total = 0;
       for (int r = -1; r < reps; ++r)
       {
         AMCL_CUDA_TRY(cudaMemsetAsync(b->acc.p, 0, static_cast<size_t>(b->max_filters) * ACC_WORDS * 8, s));
-        AMCL_CUDA_TRY(cudaMemsetAsync(b->counter.p, 0, N_CLASSES * sizeof(unsigned int), s));
+        AMCL_CUDA_TRY(cudaMemsetAsync(b->counter.p, 0, 2 * N_CLASSES * sizeof(unsigned int), s));
         cudaEventRecord(e0, s);
-        if ((rc = launch_weight_classes(b, d, t, c, s)))
+        if ((rc = launch_weight_classes(b, d, t, c, s, b->class_mask)))
           return rc;
         cudaEventRecord(e1, s);
         AMCL_CUDA_TRY(cudaEventSynchronize(e1));
@@ -1188,11 +1560,7 @@ extern "C" int amcl_batch_autotune(amcl_batch_t b, int reps, int* best_threads, 
   AMCL_CUDA_TRY(cudaStreamSynchronize(s));
   b->threads = bt;
   b->chunk = bc;
-  if (b->exec)
-  {
-    cudaGraphExecDestroy(b->exec);
-    b->exec = nullptr;
-  }
+  b->drop_graphs();
   if (best_threads)
     *best_threads = bt;
   if (best_chunk)

@@ -102,7 +102,7 @@ __device__ __forceinline__ void make_partxf(const GridView& g, float sr, float c
   {
     const double off = __dsub_rn(static_cast<double>(t[a]), g.min[a]);  // Grid3d.cpp:155-157
     p.off[a] = off;
-    p.H[a] = __double2float_rn(off);
+    p.H[a] = fadd(__double2float_rn(off), 0.0f);  // -0.0 becomes +0.0: the same cell, never a -0.0 sum
     p.L[a] = __double2float_rn(__dsub_rn(off, static_cast<double>(p.H[a])));
   }
   p.exact = (p.off[0] == static_cast<double>(p.H[0]) && p.off[1] == static_cast<double>(p.H[1]) &&
@@ -126,22 +126,22 @@ __device__ __forceinline__ int locate_pair(float X, const float2* T2, float V, f
 // Same result as locate_pair for an exact X, reading the table only near a cell
 // boundary.  q = fl32(X * fl32(1/res)) is within |q| * 2^-23 of X / res, and the
 // reference's floor(fl64(X / res)) differs from floor(X / res) only within 2^-53
-// relative of an integer; so when q is at least eps = (size + 2) * 2^-22 away from the
-// nearest integer, floor(q) is the reference's cell.  Otherwise (about 2 eps of the
-// points per axis) the pair table settles it.
-// floor(q) without a float->int conversion: adding 1.5 * 2^23 rounds q to the nearest
-// integer n (the sum lies in [2^23, 2^24), where floats are the integers), read off
-// the sum's bit pattern; d = q - n is exact and floor(q) = n - (d < 0).  This holds for
-// 0 <= q < 2^22; X >= 0 (the reference's lower bound check) keeps q >= 0, X < V keeps
-// q below size + 1, and a size of 2^22 - 2 or more makes eps >= 1, sending every
-// point to the table.  near = |d| < eps.
+// relative of an integer; so when the fraction of q is at least eps =
+// (size + 2) * 2^-22 away from 0 and 1, floor(q) is the reference's cell.  Otherwise
+// (about 2 eps of the points per axis) the pair table settles it (near is set).
+// floor(q) without a float->int conversion: adding 1.5 * 2^23 rounded toward -inf
+// gives 1.5 * 2^23 + floor(q) exactly (the sum lies in [2^23, 2^24), where floats are
+// the integers), read off the sum's bit pattern; the fraction q - floor(q) is exact.
+// This holds for 0 <= q < 2^22: X >= 0 keeps q >= 0, X < V keeps q below size + 1,
+// and a size of 2^22 - 2 or more makes eps >= 1, sending every point to the table.
+// 1 - eps is exact (eps is a multiple of 2^-22).
 __device__ __forceinline__ int floor_near(float X, float inv_res, float eps, bool& near)
 {
   const float q = fmul(X, inv_res);
-  const float r = fadd(q, 12582912.0f);
-  const float d = fsub(q, fsub(r, 12582912.0f));
-  near = fabsf(d) < eps;
-  return (__float_as_int(r) - 0x4B400000) - (d < 0.0f ? 1 : 0);
+  const float r = __fadd_rd(q, 12582912.0f);
+  const float fr = fsub(q, fsub(r, 12582912.0f));
+  near |= (fr < eps) | (fr > 1.0f - eps);
+  return __float_as_int(r) - 0x4B400000;
 }
 
 // True when a threshold lies within m of X (the estimate may then be on the wrong side).
@@ -218,10 +218,10 @@ __device__ __forceinline__ uint32_t cell_of_point(const GridView& g, const float
     for (int a = 0; a < 3; ++a)
     {
       X[a] = fadd(s[a], p.H[a]);
-      bool na;
-      k[a] = floor_near(X[a], g.inv_res[a], g.eps[a], na);
-      near |= na;
-      valid &= (X[a] >= 0.0f) & (X[a] < g.V[a]);  // NaN fails both
+      k[a] = floor_near(X[a], g.inv_res[a], g.eps[a], near);
+      // 0 <= X < V as one unsigned compare of the bit patterns: X is never -0.0 (H is
+      // canonicalised), negative X and NaN have patterns above V's
+      valid &= __float_as_uint(X[a]) < __float_as_uint(g.V[a]);
     }
     if (near)
     {

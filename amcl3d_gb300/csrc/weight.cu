@@ -33,7 +33,7 @@ constexpr int WT_THREADS = 256;
 constexpr int WT_CHUNK = 1024;  // points staged per block iteration (16 KB)
 
 template <int STORAGE, int SUM>
-__global__ __launch_bounds__(WT_THREADS, 4) void k_weight_fused(WeightArgs a, GridView g)
+__global__ __launch_bounds__(WT_THREADS, 3) void k_weight_fused(WeightArgs a, GridView g)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   float4* s_pts = reinterpret_cast<float4*>(smem);
@@ -58,31 +58,6 @@ struct __align__(16) PartRec
   PartXf xf;
   int inm;
 };
-
-template <int STORAGE, int MODE>
-__device__ __forceinline__ void tile_values(const float4* s_pts, uint32_t k0, uint32_t cnt, const float2* s_tab,
-                                            const GridView& g, const PartXf& xf, float* out, uint32_t base)
-{
-  for (uint32_t kk = 0; kk < TP_PTS_PER_WARP; kk += UNROLL)
-  {
-    uint32_t cell[UNROLL];
-#pragma unroll
-    for (int j = 0; j < UNROLL; ++j)
-    {
-      const float4 s = s_pts[k0 + kk + j];
-      cell[j] = cell_of_point<MODE>(g, s_tab, xf, s.x, s.y, s.z);
-    }
-#pragma unroll
-    for (int j = 0; j < UNROLL; ++j)
-    {
-      const uint32_t k = k0 + kk + j;
-      if (k >= cnt)
-        continue;
-      const float v = cell[j] != 0xFFFFFFFFu ? gather_prob<STORAGE>(g, cell[j]) : -1.0f;
-      out[static_cast<uint64_t>(base + k) * 32] = v;
-    }
-  }
-}
 
 template <int STORAGE>
 __global__ __launch_bounds__(TP_WARPS * 32) void k_weight_tile_vals(WeightArgs a, GridView g)
@@ -126,11 +101,11 @@ __global__ __launch_bounds__(TP_WARPS * 32) void k_weight_tile_vals(WeightArgs a
   float* out = a.scratch + (static_cast<uint64_t>(tile) * a.N) * 32 + lane;
   const uint32_t k0 = wid * TP_PTS_PER_WARP;
   if (warp_exact && a.yaw_only)
-    tile_values<STORAGE, XF_YAW>(s_pts, k0, cnt, s_tab, g, rec.xf, out, base);
+    tile_values<STORAGE, XF_YAW>(s_pts, k0, TP_PTS_PER_WARP, cnt, s_tab, g, rec.xf, out, base);
   else if (warp_exact)
-    tile_values<STORAGE, XF_EXACT>(s_pts, k0, cnt, s_tab, g, rec.xf, out, base);
+    tile_values<STORAGE, XF_EXACT>(s_pts, k0, TP_PTS_PER_WARP, cnt, s_tab, g, rec.xf, out, base);
   else
-    tile_values<STORAGE, XF_GENERAL>(s_pts, k0, cnt, s_tab, g, rec.xf, out, base);
+    tile_values<STORAGE, XF_GENERAL>(s_pts, k0, TP_PTS_PER_WARP, cnt, s_tab, g, rec.xf, out, base);
 }
 
 constexpr int TR_STAGE_PTS = 128;  // points per stage: 128 x 32 lanes x 4 B = 16 KB

@@ -85,6 +85,63 @@ __device__ __forceinline__ void weigh_chunk(const float4* s_pts, uint32_t cnt, c
   }
 }
 
+// Point-parallel weighting (a warp = 32 particles, one per lane, over `npts` staged
+// points from k0): each lane writes its particle's cell probability, or -1 for a
+// point the reference skips, to out[(base + k) * 32] for k < cnt, the
+// [tile][point][lane] slab that an in-order pass sums afterwards.
+template <int STORAGE, int MODE>
+__device__ __forceinline__ void tile_values(const float4* s_pts, uint32_t k0, uint32_t npts, uint32_t cnt,
+                                            const float2* s_tab, const GridView& g, const PartXf& xf, float* out,
+                                            uint32_t base)
+{
+  for (uint32_t kk = 0; kk < npts; kk += UNROLL)
+  {
+    uint32_t cell[UNROLL];
+#pragma unroll
+    for (int j = 0; j < UNROLL; ++j)
+    {
+      const float4 s = s_pts[k0 + kk + j];
+      cell[j] = cell_of_point<MODE>(g, s_tab, xf, s.x, s.y, s.z);
+    }
+#pragma unroll
+    for (int j = 0; j < UNROLL; ++j)
+    {
+      const uint32_t k = k0 + kk + j;
+      if (k >= cnt)
+        continue;
+      const float v = cell[j] != 0xFFFFFFFFu ? gather_prob<STORAGE>(g, cell[j]) : -1.0f;
+      out[static_cast<uint64_t>(base + k) * 32] = v;
+    }
+  }
+}
+
+// The in-order pass over one lane's column of a [point][lane] slab of n points:
+// the reference's running sum of the probabilities (skipped points are -1).  Loads
+// bypass L1 (the slab was written by other blocks).
+template <int SUM>
+__device__ __forceinline__ void slab_sum(const float* slab, uint32_t n, CloudSum<SUM>& acc)
+{
+  constexpr uint32_t U = 16;
+  uint32_t k = 0;
+  for (; k + U <= n; k += U)
+  {
+    float v[U];
+#pragma unroll
+    for (uint32_t j = 0; j < U; ++j)
+      v[j] = __ldcg(slab + static_cast<uint64_t>(k + j) * 32);
+#pragma unroll
+    for (uint32_t j = 0; j < U; ++j)
+      if (v[j] >= 0.0f)
+        acc.add(v[j]);
+  }
+  for (; k < n; ++k)
+  {
+    const float v = __ldcg(slab + static_cast<uint64_t>(k) * 32);
+    if (v >= 0.0f)
+      acc.add(v);
+  }
+}
+
 // Block-wide exact sums of (a, b) added to the grid-wide digit accumulators.
 __device__ __forceinline__ void block_exact_pair(float va, float vb, bool take, unsigned long long* acc_a,
                                                  unsigned long long* acc_b, X320* s_part)

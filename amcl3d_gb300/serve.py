@@ -7,7 +7,9 @@ sessions join and leave at a fixed rate, new sessions wait in an admission queue
 while the memory budget is exhausted; it reports p50/p99 update latency and the
 aggregate particle x point weights per second.  ``run_plain`` serves the same kind
 of requests one filter per call (predict, update, getMean, resample per request,
-one after another) for comparison on the same GPU.
+one after another) for comparison on the same GPU, closed-loop (its capacity) and
+``run_plain_open`` at the served run's offered load (open-loop arrivals, one filter
+per session, requests handled first come first served).
 """
 
 from __future__ import annotations
@@ -283,3 +285,71 @@ def run_plain(grids, pools, n_requests: int, p_range=(1000, 100000), n_range=(50
     lat = np.array(lat)
     return {"weights_per_s": weights / dt, "p50_ms": float(np.percentile(lat, 50) * 1e3),
             "p99_ms": float(np.percentile(lat, 99) * 1e3), "requests": n_requests}
+
+
+def run_plain_open(grids, pools, n_sessions: int, rate_hz: float, duration_s: float, p_range=(1000, 100000),
+                   n_range=(500, 10000), seed=0, warmup_s=1.0, odom=None, max_queue=4):
+    """The served workload without the server: one plain ParticleFilter per session,
+    open-loop Poisson arrivals at rate_hz per session, requests handled one at a time
+    in arrival order (predict, update, getMean, resample).  Latency runs from the
+    request's arrival to its mean being read; a session with max_queue requests
+    waiting drops the next scan, as the served run does."""
+    import collections
+
+    from . import synth as S
+
+    rng = np.random.default_rng(seed)
+    odom = odom if odom is not None else (*S.ODOM_MODS, 0.05, 0.0, 0.0, 0.01)
+    sessions = {}
+    for sid in range(n_sessions):
+        gi = int(rng.integers(len(grids)))
+        pose, scan, rg = pools[gi][int(rng.integers(len(pools[gi])))]
+        P = log_uniform_int(rng, *p_range)
+        n = min(log_uniform_int(rng, *n_range), scan.shape[0])
+        pf = ParticleFilter(seed=seed * 1000 + sid + 1)
+        pf.init(P, pose[0], pose[1], pose[2], pose[3], 0.3, 0.3, 0.05, 0.1)
+        sessions[sid] = (pf, grids[gi], scan[:n], rg, P * n)
+    pf, g, sc, rg, _ = sessions[0]
+    pf.predict(*odom)
+    pf.update(g, sc, rg, 0.5, 0.1, 0.0, 0.0)
+    pf.getMean()
+    pf.resample()
+    t0 = time.perf_counter()
+    events = [(t0 + rng.exponential(1.0 / rate_hz), sid) for sid in sessions]
+    heapq.heapify(events)
+    fifo = collections.deque()
+    waiting = collections.Counter()
+    lat, weights, done_req, dropped = [], 0, 0, 0
+    t_meas, t_end = t0 + warmup_s, t0 + warmup_s + duration_s
+    while True:
+        now = time.perf_counter()
+        if now >= t_end:
+            break
+        while events and events[0][0] <= now:
+            t, sid = heapq.heappop(events)
+            if waiting[sid] >= max_queue:
+                dropped += 1
+            else:
+                fifo.append((t, sid))
+                waiting[sid] += 1
+            heapq.heappush(events, (t + rng.exponential(1.0 / rate_hz), sid))
+        if not fifo:
+            time.sleep(min(max(events[0][0] - now, 0.0), 0.0005))
+            continue
+        t_arr, sid = fifo.popleft()
+        pf, g, sc, rg, w = sessions[sid]
+        pf.predict(*odom)
+        pf.update(g, sc, rg, 0.5, 0.1, 0.0, 0.0)
+        pf.getMean()
+        pf.resample()
+        td = time.perf_counter()
+        waiting[sid] -= 1
+        if td >= t_meas:
+            lat.append(td - t_arr)
+            weights += w
+            done_req += 1
+    lat = np.array(lat)
+    return {"weights_per_s": weights / duration_s, "requests": done_req, "dropped_behind": dropped,
+            "backlog_at_end": len(fifo),
+            "p50_ms": float(np.percentile(lat, 50) * 1e3) if lat.size else None,
+            "p99_ms": float(np.percentile(lat, 99) * 1e3) if lat.size else None}

@@ -6,14 +6,19 @@ One step = predict + update (cloud weights, range weights, blend, normalise, mea
 node runs per accepted scan (Node.cpp:154-182).  Metric: particle x point weights
 per second (P * N per step / step time), whole job.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--config warehouse|room]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--config warehouse|hall|room|served]
                   [--impl ours|reference]
 
 `value` times the steps with the scan already resident in HBM (CUDA events on the
 filter's stream); `e2e` times the same steps through the C ABI with host buffers
 (the scan copied host->device and the mean read back every step).  The default
 workload is the large single-filter configuration (2000x2000x400-cell warehouse,
-200k particles, 20k points); `room` is the CPU-runnable 400x400x100 case.
+200k particles, 20k points); `room` is the CPU-runnable 400x400x100 case, `hall`
+the warehouse's filter on a 410 MB grid (profiler captures), `served` the
+multi-session server under open-loop load.  `--impl reference` times the
+reference's CPU update arithmetic (the oracle's C restatement) on the host cores on
+the same workload; its grid is built on the host (where the reference's 250 M-cell
+limit rules out a full build, only the cells its timed sample reads).
 Multi-GPU runs are independent replicas (one filter per GPU, no collective on the
 data path), launched one process per GPU by torchrun.
 """
@@ -152,29 +157,50 @@ class ClockSampler:
 
 # ---- CPU baseline: the oracle's restatement of the reference, on host threads --------------------
 
-def cpu_baseline(occ_points, info, scans, ranges, parts, seconds: float, threads: int | None = None,
-                 gpu_grid=None):
-    """Times the reference's update arithmetic (oracle restatement, float running
-    sums, libm trig/exp) on a particle sample, all host cores.  Returns (rate, desc)."""
-    import oracle as O
+REF_CELL_LIMIT = 250_000_000  # computeGrid refuses larger grids (PointCloudTools.cpp:103-105)
+REF_SAMPLE = 16384             # particles of the reference path's timed sample
 
-    threads = threads or os.cpu_count() or 1
-    size = info["dims"]
-    if gpu_grid is not None:
-        d, p = gpu_grid.read_cells()
-    else:
-        d, p = O.compute_grid(occ_points, info["min"], info["max"], info["res"], 0.05, exp_mode=0)
-    g = O.GridData(info["min"], info["max"], info["res"], size, p.ravel(), d.ravel())
-    del d
-    scan = scans[0]
-    N = scan.shape[0]
+
+def cpu_update_timer(g, scan, rng, threads: int):
+    """run(sample): the reference's update arithmetic (oracle restatement, float running
+    sums, libm trig/exp) over a particle sample, split over host threads."""
+    import oracle as O
 
     def run(sample: np.ndarray):
         chunks = np.array_split(sample, threads)
         with ThreadPoolExecutor(threads) as ex:
-            list(ex.map(lambda c: O.update_f32(c, g, scan, ranges[0], 0.5, 0.1, 0.0, 0.0, yaw_trig=0, exp_mode=0)
+            list(ex.map(lambda c: O.update_f32(c, g, scan, rng, 0.5, 0.1, 0.0, 0.0, yaw_trig=0, exp_mode=0)
                         if len(c) else None, chunks))
 
+    return run
+
+
+def time_sample(run, sample, N, seconds):
+    """Repeats the sample until about half of `seconds` has passed; weights/s."""
+    reps = 0
+    t0 = time.perf_counter()
+    while True:
+        run(sample)
+        reps += 1
+        dt = time.perf_counter() - t0
+        if dt >= 0.5 * seconds or reps >= 1000:
+            break
+    return reps * sample.shape[0] * N / dt, reps, dt
+
+
+def cpu_baseline(occ_points, info, scans, ranges, parts, seconds: float, threads: int | None = None,
+                 gpu_grid=None):
+    """Times the reference's update arithmetic on a particle sample, all host cores, on
+    the grid read back from the GPU.  Returns (rate, desc)."""
+    import oracle as O
+
+    threads = threads or os.cpu_count() or 1
+    d, p = gpu_grid.read_cells()
+    g = O.GridData(info["min"], info["max"], info["res"], info["dims"], p.ravel(), d.ravel())
+    del d
+    scan = scans[0]
+    N = scan.shape[0]
+    run = cpu_update_timer(g, scan, ranges[0], threads)
     # calibrate on a small sample, then size the timed sample to ~`seconds`
     cal = parts[: max(threads * 4, 64)]
     t0 = time.perf_counter()
@@ -182,21 +208,52 @@ def cpu_baseline(occ_points, info, scans, ranges, parts, seconds: float, threads
     dt = max(time.perf_counter() - t0, 1e-4)
     rate = cal.shape[0] * N / dt
     n_sample = int(min(parts.shape[0], max(threads * 8, rate * seconds / N)))
-    sample = parts[:n_sample]
-    reps = 0
-    t0 = time.perf_counter()
-    while True:  # repeat small samples until the bounded duration is reached
-        run(sample)
-        reps += 1
-        dt = time.perf_counter() - t0
-        if dt >= 0.5 * seconds or reps >= 1000:
-            break
-    return reps * n_sample * N / dt, {
+    rate, reps, dt = time_sample(run, parts[:n_sample], N, seconds)
+    return rate, {
         "cores": threads,
         "kind": "port",
         "sample": f"{reps} x {n_sample} of {parts.shape[0]} particles x {N} points "
                   f"(C restatement of ParticleFilter::update with float running sums), {dt:.1f}s",
     }
+
+
+def reference_grid(occ_points, info, sample, scan, threads: int):
+    """The grid the reference's CPU path reads, built on the host by the oracle's
+    restatement of computeGrid: in full where the reference can build it itself, else
+    (the warehouse's 1.6 G cells exceed its 250 M limit and would take hours on the
+    host) only the cells the sample's weighting reads, every other cell left 0."""
+    import oracle as O
+
+    size = tuple(int(v) for v in info["dims"])
+    cells = int(np.prod(size))
+    if cells <= REF_CELL_LIMIT:
+        d, p = O.compute_grid(occ_points, info["min"], info["max"], info["res"], 0.05, exp_mode=0, threads=threads)
+        return O.GridData(info["min"], info["max"], info["res"], size, p.ravel(), d.ravel()), "full"
+    prob = np.zeros(cells, np.float32)  # pages are mapped only where written
+    g = O.GridData(info["min"], info["max"], info["res"], size, prob)
+    mark = np.zeros(cells, np.uint8)
+    chunks = [sample[k:k + 256, :4] for k in range(0, sample.shape[0], 256)]
+
+    def touched(c):
+        _, cl = O.cloud_weights(g, c, scan, 0.0, 0.0, yaw_trig=0, cells=True)
+        return np.unique(cl[cl >= 0])
+
+    with ThreadPoolExecutor(threads) as ex:
+        for u in ex.map(touched, chunks):
+            mark[u] = 1
+    idx = np.flatnonzero(mark).astype(np.uint64)
+    del mark
+    prob[idx] = O.grid_cell_probs(occ_points, info["min"], info["res"], 0.05, size, idx, exp_mode=0, threads=threads)
+    return g, f"{idx.size} cells read by the sample (of {cells})"
+
+
+def reference_config(cfg, info, n_points_mean, world):
+    """The `config` object of both arms' JSON lines."""
+    cells = int(np.prod(info["dims"]))
+    return {"workload": cfg["workload"], "particles": cfg["P"], "points": int(n_points_mean), "grid_cells": cells,
+            "beacons": cfg["B"], "parallelism": f"replicas x{world}",
+            "l2": "flushed between steps (512 MB write)" if cells * 4 < 200 * 2**20 else
+                  f"grid larger than L2 ({cells * 4 / 1e9:.2f} GB FP32)"}
 
 
 # ---- our arm -----------------------------------------------------------------------------------
@@ -318,10 +375,7 @@ def run_ours(args, cfg, rank, world, local_rank):
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded room/warehouse maps, ray-cast scans; no public dataset)",
-        "config": {"workload": cfg["workload"], "particles": P, "points": int(N_mean), "grid_cells":
-                   int(np.prod(info["dims"])), "beacons": cfg["B"], "parallelism": f"replicas x{world}",
-                   "l2": "flushed between steps (512 MB write)" if l2_small else
-                         f"grid larger than L2 ({np.prod(info['dims']) * 4 / 1e9:.2f} GB FP32)", "grid_build_s": round(build_s, 3)},
+        "config": reference_config(cfg, info, N_mean, world), "grid_build_s": round(build_s, 3),
         "e2e": {"value": e2e_total / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(gpu_launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -382,10 +436,15 @@ def voxel_section(seed: int, leaf: float = 0.1, reps: int = 20):
             "gpu_points_per_s": raw.shape[0] / (gpu_ms / 1e3)}
 
 
+PLAIN_OPEN_MAX_SESSIONS = 400  # one plain filter (with its own weighting scratch) per session
+
+
 def served_vs_plain(grids, maps, n_sessions, rate_hz, duration_s, churn_per_s, seed=7,
                     p_range=(1000, 100000), n_range=(500, 10000), plain_requests=400):
-    """Sessions served with continuous batching vs the same request mix one filter per
-    call, on the same GPU.  Returns the "served" JSON object."""
+    """Sessions served with continuous batching vs the same sessions each on its own
+    plain filter (requests first come first served, one at a time) at the same offered
+    load, on the same GPU; plus the plain path's closed-loop capacity.  Returns the
+    "served" JSON object."""
     from amcl3d_gb300 import serve as SV
 
     pools = SV.make_scan_pool(maps, seed, n_range[1])
@@ -397,8 +456,13 @@ def served_vs_plain(grids, maps, n_sessions, rate_hz, duration_s, churn_per_s, s
     served = SV.run_load(srv, grids, pools, n_sessions, rate_hz, duration_s, churn_per_s, p_range, n_range, seed=seed)
     log(f"served {n_sessions} sessions in {time.perf_counter() - t0:.1f}s: {served}")
     srv.close()
+    if n_sessions <= PLAIN_OPEN_MAX_SESSIONS:
+        plain_open = SV.run_plain_open(grids, pools, n_sessions, rate_hz, duration_s, p_range, n_range, seed=seed)
+        log(f"plain, same load: {plain_open}")
+    else:
+        plain_open = {"skipped": f"more than {PLAIN_OPEN_MAX_SESSIONS} plain filters (per-filter scratch)"}
     plain = SV.run_plain(grids, pools, plain_requests, p_range, n_range, seed=seed)
-    log(f"plain: {plain}")
+    log(f"plain, closed loop: {plain}")
     return {
         "sessions": n_sessions, "rate_hz_per_session": rate_hz, "duration_s": duration_s,
         "churn_per_s": churn_per_s, "particles": f"log-uniform {p_range}", "points": f"log-uniform {n_range}",
@@ -408,9 +472,9 @@ def served_vs_plain(grids, maps, n_sessions, rate_hz, duration_s, churn_per_s, s
         "weights_per_s": served["weights_per_s"], "p50_ms": served["p50_ms"], "p99_ms": served["p99_ms"],
         "mean_batch": served["mean_batch"], "requests": served["requests_measured"],
         "dropped_behind": served["dropped_behind"], "admission_waiting": served["admission_waiting"],
-        "plain_weights_per_s": plain["weights_per_s"], "plain_p50_ms": plain["p50_ms"],
-        "plain_p99_ms": plain["p99_ms"],
-        "served_over_plain": served["weights_per_s"] / plain["weights_per_s"],
+        "plain_same_load": plain_open,
+        "plain_capacity_weights_per_s": plain["weights_per_s"], "plain_closed_loop_p50_ms": plain["p50_ms"],
+        "plain_closed_loop_p99_ms": plain["p99_ms"],
     }
 
 
@@ -441,22 +505,36 @@ def run_served(args, rank, world, local_rank):
 
 def run_reference(args, cfg, rank, world):
     """The reference's CPU path (its arithmetic, restated in C: the reference tree
-    cannot travel to this host) on all host cores, a bounded sample per step."""
+    cannot travel to this host) on all host cores, a bounded sample per step, on the
+    same workload as our arm (same seeds)."""
     if rank != 0:
         return None
+    threads = os.cpu_count() or 1
     occ_points, info, scans, ranges, odos, parts = make_workload(cfg, 1000)
-    rates = []
-    desc = None
+    sample = parts[: min(parts.shape[0], REF_SAMPLE)]
+    t0 = time.perf_counter()
+    g, grid_desc = reference_grid(occ_points, info, sample, scans[0], threads)
+    log(f"reference grid ({grid_desc}) in {time.perf_counter() - t0:.1f}s")
+    N = scans[0].shape[0]
+    run = cpu_update_timer(g, scans[0], ranges[0], threads)
+    rates, reps_total, dt_total = [], 0, 0.0
     for k in range(args.warmup + args.steps):
-        rate, desc = cpu_baseline(occ_points, info, scans, ranges, parts, seconds=args.cpu_seconds / 4)
+        rate, reps, dt = time_sample(run, sample, N, args.cpu_seconds / 4)
         if k >= args.warmup:
             rates.append(rate)
+            reps_total += reps
+            dt_total += dt
     value = float(np.mean(rates))
+    desc = {"cores": threads, "kind": "port",
+            "sample": f"{args.steps} steps x {reps_total // max(args.steps, 1)} x {sample.shape[0]} of "
+                      f"{parts.shape[0]} particles x {N} points (C restatement of ParticleFilter::update with "
+                      f"float running sums), {dt_total:.1f}s; grid: {grid_desc}"}
     return {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": cfg["workload"], "particles": cfg["P"], "points": cfg["N"]},
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": (sample.shape[0] * N / value) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded room/warehouse maps, ray-cast scans; no public dataset)",
+        "config": reference_config(cfg, info, float(np.mean([sc.shape[0] for sc in scans])), world),
         "cpu_baseline": {"value": value, "unit": UNIT, **desc},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -514,7 +592,10 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.config == "served":
         if rank == 0:
-            print(json.dumps(run_served(args, rank, 1, local_rank)), flush=True)
+            out = ({"impl": "reference", "unavailable": "the reference serves one filter per ROS node; it has no "
+                    "multi-session server to time"} if args.impl == "reference" else
+                   run_served(args, rank, 1, local_rank))
+            print(json.dumps(out), flush=True)
         return
     cfg = CONFIGS[args.config]
     if args.impl == "reference":

@@ -302,6 +302,13 @@ int amcl_batch_get_mean(amcl_batch_t b, int slot, float mean7[7], double mean_va
 /* Shape of the weighting kernel: particle tile (threads per block: 64, 128, 256, 512)
  * and point tile (scan points staged in shared memory per iteration). */
 int amcl_batch_set_tuning(amcl_batch_t b, int threads, int chunk);
+
+/* Point-parallel weighting of small steps: mode 0 (default) splits every filter's
+ * scan over the SMs when the step's particle tiles cannot fill the GPU, 1 never
+ * splits, 2 always splits (when the probability slabs fit).  scratch_bytes (0: keep;
+ * default 4 GiB) bounds the slab memory a split step may allocate.  Results are the
+ * same either way. */
+int amcl_batch_set_split(amcl_batch_t b, int mode, uint64_t scratch_bytes);
 int amcl_batch_get_tuning(amcl_batch_t b, int* threads, int* chunk);
 /* Times the weighting phase of the last step under each candidate (particle tile x
  * point tile) shape, `reps` runs each, keeps the fastest and reports it.  The state of

@@ -82,6 +82,9 @@ def _load_oracle():
     lib.orc_compute_grid.restype = C.c_int
     lib.orc_philox4x32_10.argtypes = [_u32p, _u32p, _u32p]
     lib.orc_philox4x32_10.restype = None
+    lib.orc_grid_cell_probs.argtypes = [_fp, C.c_uint64, C.c_uint32, _dp, C.c_double, C.c_double, _u32p,
+                                        C.POINTER(C.c_uint64), C.c_uint64, C.c_int, C.c_int, _fp]
+    lib.orc_grid_cell_probs.restype = C.c_int
     lib.orc_voxel_downsample.argtypes = [_fp, C.c_uint64, C.c_uint32, _fp, _fp, C.POINTER(C.c_uint64)]
     lib.orc_voxel_downsample.restype = C.c_int
     return lib
@@ -296,6 +299,21 @@ def compute_grid(points, mn, mx, res, sensor_dev, lo=None, hi=None, exp_mode=1, 
     if rc:
         raise RuntimeError(f"orc_compute_grid failed ({rc})")
     return dist, prob
+
+
+def grid_cell_probs(points, mn, res, sensor_dev, size, cells, exp_mode=0, threads=None) -> np.ndarray:
+    """computeGrid's prob for the given linear cell indices only (see orc_grid_cell_probs)."""
+    pts = np.ascontiguousarray(np.asarray(points, np.float32)[:, :3])
+    c = np.ascontiguousarray(cells, dtype=np.uint64)
+    out = np.empty(c.size, np.float32)
+    sz = np.ascontiguousarray(size, dtype=np.uint32)
+    mn64 = np.ascontiguousarray(mn, dtype=np.float64)
+    rc = orc.orc_grid_cell_probs(_f(pts), pts.shape[0], 3, _d(mn64), float(res),
+                                 float(sensor_dev), sz.ctypes.data_as(_u32p), c.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                 c.size, int(exp_mode), int(threads or os.cpu_count() or 1), _f(out))
+    if rc:
+        raise MemoryError("orc_grid_cell_probs")
+    return out
 
 
 def voxel_downsample(cloud, leaf):

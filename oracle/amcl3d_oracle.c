@@ -279,7 +279,10 @@ typedef struct
   int tid;
 } grid_job;
 
-static float nn_sqdist(const grid_job* J, float qx, float qy, float qz)
+/* Exact nearest squared distance; with max_d2 finite the search may stop once no
+ * point within sqrt(max_d2) remains possible (the result is then >= max_d2, possibly
+ * INFINITY). */
+static float nn_sqdist(const grid_job* J, float qx, float qy, float qz, double max_d2)
 {
   float best = INFINITY;
   const double qc[3] = { qx, qy, qz };
@@ -351,6 +354,8 @@ static float nn_sqdist(const grid_job* J, float qx, float qy, float qz)
       break;
     if (best < INFINITY && (double)best < bound * bound * (1.0 - 1e-6))
       break;
+    if (bound * bound * (1.0 - 1e-6) > max_d2)
+      break;
   }
   return best;
 }
@@ -375,37 +380,17 @@ static void* grid_worker(void* arg)
       J->prob[k] = 0.0f;
       continue;
     }
-    const float dist = nn_sqdist(J, qx, qy, qz);
+    const float dist = nn_sqdist(J, qx, qy, qz, INFINITY);
     J->dist[k] = dist;                                            /* PointCloudTools.cpp:136 */
     J->prob[k] = J->c1 * exp_f(-dist * dist * J->c2, J->exp_mode); /* PointCloudTools.cpp:137 */
   }
   return NULL;
 }
 
-int orc_compute_grid(const float* xyz, uint64_t n, uint32_t stride, const double min[3], const double max[3],
-                     double res, double sensor_dev, const uint32_t lo[3], const uint32_t hi[3], int exp_mode,
-                     int threads, float* dist, float* prob)
+/* The point buckets of the exact search (cube side h: twice the mean point spacing). */
+static int build_buckets(grid_job* J, const float* xyz, uint64_t n, uint32_t stride)
 {
-  grid_job base;
-  memset(&base, 0, sizeof(base));
-  base.xyz = xyz;
-  base.n = n;
-  base.stride = stride;
-  base.res = res;
-  base.c1 = (float)(1. / (sensor_dev * sqrt(2 * M_PI))); /* PointCloudTools.cpp:114 */
-  base.c2 = (float)(1. / (2. * sensor_dev * sensor_dev)); /* PointCloudTools.cpp:115 */
-  base.exp_mode = exp_mode;
-  base.dist = dist;
-  base.prob = prob;
-  for (int a = 0; a < 3; ++a)
-  {
-    base.min[a] = min[a];
-    base.qlo[a] = lo[a];
-    base.qhi[a] = hi[a];
-    if (hi[a] < lo[a])
-      return -1;
-  }
-  (void)max;
+  grid_job base = *J;
   uint32_t* cell = NULL;
   if (n)
   {
@@ -468,6 +453,37 @@ int orc_compute_grid(const float* xyz, uint64_t n, uint32_t stride, const double
       base.order[fill[cell[i]]++] = (uint32_t)i;
     free(fill);
   }
+  free(cell);
+  *J = base;
+  return 0;
+}
+
+int orc_compute_grid(const float* xyz, uint64_t n, uint32_t stride, const double min[3], const double max[3],
+                     double res, double sensor_dev, const uint32_t lo[3], const uint32_t hi[3], int exp_mode,
+                     int threads, float* dist, float* prob)
+{
+  grid_job base;
+  memset(&base, 0, sizeof(base));
+  base.xyz = xyz;
+  base.n = n;
+  base.stride = stride;
+  base.res = res;
+  base.c1 = (float)(1. / (sensor_dev * sqrt(2 * M_PI))); /* PointCloudTools.cpp:114 */
+  base.c2 = (float)(1. / (2. * sensor_dev * sensor_dev)); /* PointCloudTools.cpp:115 */
+  base.exp_mode = exp_mode;
+  base.dist = dist;
+  base.prob = prob;
+  for (int a = 0; a < 3; ++a)
+  {
+    base.min[a] = min[a];
+    base.qlo[a] = lo[a];
+    base.qhi[a] = hi[a];
+    if (hi[a] < lo[a])
+      return -1;
+  }
+  (void)max;
+  if (build_buckets(&base, xyz, n, stride))
+    return -2;
   if (threads < 1)
     threads = 1;
   grid_job* jobs = (grid_job*)malloc(sizeof(grid_job) * threads);
@@ -485,7 +501,88 @@ int orc_compute_grid(const float* xyz, uint64_t n, uint32_t stride, const double
   free(th);
   free(base.start);
   free(base.order);
-  free(cell);
+  return 0;
+}
+
+/* ---- prob of chosen cells --------------------------------------------------------------- */
+
+typedef struct
+{
+  grid_job J;
+  const uint64_t* cells;
+  uint64_t m;
+  uint32_t size[3];
+  double max_d2;
+} cells_job;
+
+static void* cells_worker(void* arg)
+{
+  const cells_job* C = (const cells_job*)arg;
+  const grid_job* J = &C->J;
+  const uint64_t sxy = (uint64_t)C->size[0] * C->size[1];
+  for (uint64_t k = J->tid; k < C->m; k += J->nthreads)
+  {
+    const uint64_t idx = C->cells[k];
+    const uint32_t ix = (uint32_t)(idx % C->size[0]);
+    const uint32_t iy = (uint32_t)((idx / C->size[0]) % C->size[1]);
+    const uint32_t iz = (uint32_t)(idx / sxy);
+    const float qx = J->min[0] + (ix * J->res); /* PointCloudTools.cpp:127-129 */
+    const float qy = J->min[1] + (iy * J->res);
+    const float qz = J->min[2] + (iz * J->res);
+    if (J->n == 0)
+    {
+      J->prob[k] = 0.0f;
+      continue;
+    }
+    const float dist = nn_sqdist(J, qx, qy, qz, C->max_d2);
+    J->prob[k] = (double)dist >= C->max_d2 ? 0.0f : J->c1 * exp_f(-dist * dist * J->c2, J->exp_mode);
+  }
+  return NULL;
+}
+
+int orc_grid_cell_probs(const float* xyz, uint64_t n, uint32_t stride, const double min[3], double res,
+                        double sensor_dev, const uint32_t size[3], const uint64_t* cells, uint64_t m, int exp_mode,
+                        int threads, float* prob)
+{
+  cells_job base;
+  memset(&base, 0, sizeof(base));
+  base.J.xyz = xyz;
+  base.J.n = n;
+  base.J.stride = stride;
+  base.J.res = res;
+  base.J.c1 = (float)(1. / (sensor_dev * sqrt(2 * M_PI))); /* PointCloudTools.cpp:114 */
+  base.J.c2 = (float)(1. / (2. * sensor_dev * sensor_dev)); /* PointCloudTools.cpp:115 */
+  base.J.exp_mode = exp_mode;
+  base.J.prob = prob;
+  for (int a = 0; a < 3; ++a)
+  {
+    base.J.min[a] = min[a];
+    base.size[a] = size[a];
+  }
+  base.cells = cells;
+  base.m = m;
+  /* beyond d^2 = sqrt(120 / c2) the float product d^2*d^2*c2 exceeds 120 and expf
+   * underflows to 0 (it is 0 above 103.98): the cell's prob is 0 without the exact d */
+  base.max_d2 = sqrt(120.0 / (double)base.J.c2);
+  if (build_buckets(&base.J, xyz, n, stride))
+    return -2;
+  if (threads < 1)
+    threads = 1;
+  cells_job* jobs = (cells_job*)malloc(sizeof(cells_job) * threads);
+  pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * threads);
+  for (int t = 0; t < threads; ++t)
+  {
+    jobs[t] = base;
+    jobs[t].J.nthreads = threads;
+    jobs[t].J.tid = t;
+    pthread_create(&th[t], NULL, cells_worker, &jobs[t]);
+  }
+  for (int t = 0; t < threads; ++t)
+    pthread_join(th[t], NULL);
+  free(jobs);
+  free(th);
+  free(base.J.start);
+  free(base.J.order);
   return 0;
 }
 

@@ -76,6 +76,14 @@ int orc_compute_grid(const float* xyz, uint64_t n, uint32_t stride, const double
 int orc_voxel_downsample(const float* xyz, uint64_t n, uint32_t stride, const float leaf[3], float* out4,
                          uint64_t* n_out);
 
+/* prob of computeGrid (PointCloudTools.cpp:133-137) for the m listed cells (linear
+ * indices ix + iy*size[0] + iz*size[0]*size[1]) only.  A cell whose nearest point lies
+ * beyond the distance where c1*expf(-d^2*d^2*c2) underflows to 0 gets 0 without an
+ * exact search (the reference's value there is 0 too). */
+int orc_grid_cell_probs(const float* xyz, uint64_t n, uint32_t stride, const double min[3], double res,
+                        double sensor_dev, const uint32_t size[3], const uint64_t* cells, uint64_t m, int exp_mode,
+                        int threads, float* prob);
+
 /* Philox4x32-10 block (Salmon et al., SC'11). */
 void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 

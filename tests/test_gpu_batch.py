@@ -1,7 +1,8 @@
 """Batched filters (amcl_batch_*): every filter stepped inside a batch computes exactly
 what the same filter computes stepped alone (same seed, same inputs), whatever the
-other filters in the step; admission against the arena budget; the autotuner keeps
-the filters' state."""
+other filters in the step and whether the step's weighting runs fused (a thread per
+particle) or split over points (slabs summed in cloud order); admission against the
+arena budget; the autotuner keeps the filters' state."""
 
 import numpy as np
 import pytest
@@ -49,8 +50,9 @@ def run_alone(amcl, grids, sp, steps):
     return out
 
 
+@pytest.mark.parametrize("split", [1, 2], ids=["fused", "split"])
 @pytest.mark.parametrize("tuning", [(256, 1024), (128, 256), (512, 2048)])
-def test_batch_equals_alone(amcl, world, tuning):
+def test_batch_equals_alone(amcl, world, tuning, split):
     from amcl3d_gb300.batch import FilterBatch
 
     grids, specs = world
@@ -58,6 +60,7 @@ def test_batch_equals_alone(amcl, world, tuning):
     alone = [run_alone(amcl, grids, sp, steps) for sp in specs]
     B = FilterBatch(max_filters=8, max_particles=40000, max_points_per_step=8000)
     B.set_tuning(*tuning)
+    B.set_split(split)  # fused tiles, or every scan split over the SMs (the 0-point filter stays fused)
     slots = []
     for sp in specs:
         sl = B.add(grids[sp["grid"]], sp["P"], sp["seed"])
