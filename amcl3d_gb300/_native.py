@@ -117,6 +117,7 @@ _SIGS = {
     "amcl_batch_capacity": [_vp, C.POINTER(_u64), C.POINTER(_u32)],
     "amcl_batch_stream": [_vp, C.POINTER(_vp)],
     "amcl_server_create": [C.POINTER(_vp), _u32, _u64, _u64, _vp],
+    "amcl_server_create_lanes": [C.POINTER(_vp), _u32, _u64, _u64, _u32, _vp],
     "amcl_server_destroy": [_vp],
     "amcl_server_open_session": [_vp, _vp, _u32, _u64, _int, _fp, C.POINTER(_i64)],
     "amcl_server_close_session": [_vp, _i64],

@@ -36,6 +36,7 @@
 #include <mutex>
 #include <vector>
 
+#include "bulk.cuh"
 #include "filter_dev.cuh"
 #include "grid.cuh"
 #include "weight_dev.cuh"
@@ -212,6 +213,7 @@ constexpr int SP_WARPS = 8;
 constexpr uint32_t SP_WARP_PTS = 64;                 // points per warp per split item
 constexpr uint32_t SP_PTS = SP_WARPS * SP_WARP_PTS;  // points per split item
 constexpr uint32_t SP_RED_PTS = 64;                  // slab points per reduction stage (8 KB)
+constexpr uint32_t SP_RED_STAGES = 4;                // reduction stages in shared memory
 
 __device__ __forceinline__ unsigned int atomic_add_acq_rel_gpu(unsigned int* p, unsigned int v)
 {
@@ -230,7 +232,7 @@ __host__ __device__ inline uint32_t split_red_offset(uint32_t tab_cap)
 // Persistent: blocks take (split step, tile * slices + slice) items of one class.
 // Each warp covers SP_WARP_PTS points of the slice for the tile's 32 particles.  The
 // block whose count completes the tile streams the tile's slab through shared memory
-// (all warps load, 8 KB per stage, double-buffered; warp 0 adds in cloud order).
+// (all warps copy, 8 KB stages, 3 in flight; warp 0 adds in cloud order).
 template <int STORAGE, int SUM>
 __global__ __launch_bounds__(SP_WARPS * 32, 3) void k_b_split(BatchDev d, uint32_t tab_cap)
 {
@@ -238,7 +240,7 @@ __global__ __launch_bounds__(SP_WARPS * 32, 3) void k_b_split(BatchDev d, uint32
   float4* s_pts = reinterpret_cast<float4*>(smem);
   float4* s_rg = s_pts + SP_PTS;
   float2* s_tab = reinterpret_cast<float2*>(s_rg + MAX_RANGES);
-  float* s_red = reinterpret_cast<float*>(smem) + split_red_offset(tab_cap);  // 2 x SP_RED_PTS x 32
+  float* s_red = reinterpret_cast<float*>(smem) + split_red_offset(tab_cap);  // SP_RED_STAGES x SP_RED_PTS x 32
   __shared__ uint32_t s_item;
   __shared__ int s_loaded;
   __shared__ int s_last;
@@ -309,36 +311,43 @@ __global__ __launch_bounds__(SP_WARPS * 32, 3) void k_b_split(BatchDev d, uint32
     __syncthreads();
     if (!s_last)
       continue;
-    // The tile's last slice: sum the slab in cloud order.
+    // The tile's last slice: sum the slab in cloud order.  Every thread copies its
+    // 16-byte pieces of the next stages with cp.async (SP_RED_STAGES - 1 in flight);
+    // warp 0 adds each landed stage.
     const float4* slab4 = reinterpret_cast<const float4*>(slab);
     const uint32_t nst = (st.N + SP_RED_PTS - 1) / SP_RED_PTS;
     constexpr uint32_t F4_PER_STAGE = SP_RED_PTS * 8;  // 32 floats per point
     constexpr uint32_t F4_PER_THREAD = F4_PER_STAGE / (SP_WARPS * 32);
     const uint32_t f4_total = st.N * 8;
     float4* red4 = reinterpret_cast<float4*>(s_red);
-#pragma unroll
-    for (uint32_t q = 0; q < F4_PER_THREAD; ++q)
-    {
-      const uint32_t f = q * SP_WARPS * 32 + threadIdx.x;
-      if (f < f4_total)
-        red4[f] = __ldcg(slab4 + f);
-    }
-    __syncthreads();
-    CloudSum<SUM> acc;
-    for (uint32_t sg = 0; sg < nst; ++sg)
-    {
-      float4 nxt[F4_PER_THREAD];
-      const uint32_t g0 = (sg + 1) * F4_PER_STAGE;
+    auto issue = [&](uint32_t sg) {
 #pragma unroll
       for (uint32_t q = 0; q < F4_PER_THREAD; ++q)
       {
-        const uint32_t f = g0 + q * SP_WARPS * 32 + threadIdx.x;
-        if (sg + 1 < nst && f < f4_total)
-          nxt[q] = __ldcg(slab4 + f);
+        const uint32_t f = q * SP_WARPS * 32 + threadIdx.x;
+        const uint32_t gidx = sg * F4_PER_STAGE + f;
+        if (gidx < f4_total)
+          cp_async16(red4 + (sg % SP_RED_STAGES) * F4_PER_STAGE + f, slab4 + gidx);
       }
+    };
+#pragma unroll
+    for (uint32_t sg = 0; sg + 1 < SP_RED_STAGES; ++sg)
+    {
+      if (sg < nst)
+        issue(sg);
+      cp_async_commit();
+    }
+    CloudSum<SUM> acc;
+    for (uint32_t sg = 0; sg < nst; ++sg)
+    {
+      if (sg + SP_RED_STAGES - 1 < nst)
+        issue(sg + SP_RED_STAGES - 1);
+      cp_async_commit();
+      cp_async_wait<SP_RED_STAGES - 1>();  // this thread's copies of stage sg have landed
+      __syncthreads();                     // everyone's have
       if (wid == 0 && rec.inm)
       {
-        const float* buf = s_red + (sg & 1) * SP_RED_PTS * 32;
+        const float* buf = s_red + (sg % SP_RED_STAGES) * SP_RED_PTS * 32;
         const uint32_t pts = min(SP_RED_PTS, st.N - sg * SP_RED_PTS);
         for (uint32_t k = 0; k < pts; ++k)
         {
@@ -347,15 +356,7 @@ __global__ __launch_bounds__(SP_WARPS * 32, 3) void k_b_split(BatchDev d, uint32
             acc.add(v);
         }
       }
-      float4* dst = red4 + ((sg + 1) & 1) * F4_PER_STAGE;
-#pragma unroll
-      for (uint32_t q = 0; q < F4_PER_THREAD; ++q)
-      {
-        const uint32_t f = g0 + q * SP_WARPS * 32 + threadIdx.x;
-        if (sg + 1 < nst && f < f4_total)
-          dst[q * SP_WARPS * 32 + threadIdx.x] = nxt[q];
-      }
-      __syncthreads();
+      __syncthreads();  // the stage's buffer is free for the copy issued next
     }
     if (wid == 0)
     {
@@ -576,7 +577,8 @@ size_t weight_smem(const amcl_batch_s* b, int chunk)
 
 size_t split_smem(const amcl_batch_s* b)
 {
-  return static_cast<size_t>(split_red_offset(b->tab_cap)) * 4 + 2ull * SP_RED_PTS * 32 * sizeof(float);
+  return static_cast<size_t>(split_red_offset(b->tab_cap)) * 4 +
+         static_cast<size_t>(SP_RED_STAGES) * SP_RED_PTS * 32 * sizeof(float);
 }
 
 // One persistent launch per weighting class in `mask` (bits 0-5: fused (storage, sum)
@@ -744,7 +746,7 @@ uint64_t weight_items_needed(const amcl_batch_s* b, int threads)
 // points) when the fused tiles cannot fill the GPU and the slabs fit the scratch
 // budget; assigns the tile counters, slab and transform offsets and sizes the buffers
 // (their reallocation drops the captured graphs).
-constexpr uint32_t SPLIT_BELOW_TILES_PER_SM = 2;
+constexpr uint32_t SPLIT_BELOW_TILES_PER_SM = 1;
 
 int plan_split(amcl_batch_s* b, int threads)
 {

@@ -1,16 +1,20 @@
-// Multi-session localisation server over a filter batch (amcl_batch_*).
+// Multi-session localisation server over filter batches (amcl_batch_*).
 //
-// Each session is one filter slot of the batch: its particles and generator state
-// stay on the device between requests.  Clients submit update requests (scan,
-// odometry increment, beacon ranges) from any thread; a scheduler thread forms the
-// batch steps: every session with a pending request contributes its oldest one.
-// Continuous batching: while step k runs on the GPU, requests that arrive are
-// staged for step k + 1, which launches as soon as step k's results have been read
-// back.  A session's requests complete in submission order (one per step).
+// Each session is one filter slot of one of the server's lanes: a lane is a batch
+// (its own stream, arenas and captured step graphs) with its own scheduler thread,
+// so the lanes' steps run concurrently on the GPU.  A session's particles and
+// generator state stay on the device between requests.  Clients submit update
+// requests (scan, odometry increment, beacon ranges) from any thread; each lane's
+// scheduler forms its batch steps: every session of the lane with a pending request
+// contributes its oldest one.  Continuous batching: while step k runs on the GPU,
+// requests that arrive are staged for step k + 1, which launches as soon as step k's
+// results have been read back.  A session's requests complete in submission order
+// (one per step).  New sessions go to the lane with the fewest sessions.
 //
-// Admission: opening a session takes a slot and a particle range of the batch's
-// fixed arenas; when they are exhausted amcl_server_open_session fails with
-// AMCL_ENOMEM and the caller retries once sessions close.
+// Admission: the server's particle budget bounds the capacity of all open sessions
+// together (each lane's arena can hold the whole budget, so a session fits in any
+// lane); beyond it amcl_server_open_session fails with AMCL_ENOMEM and the caller
+// retries once sessions close.
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -44,7 +48,9 @@ struct Request
 
 struct Session
 {
+  int lane = 0;
   int slot = -1;
+  uint64_t capacity = 0;
   std::deque<Request> pending;
   int in_flight = 0;  // staged or running requests
 };
@@ -52,14 +58,20 @@ struct Session
 
 struct amcl_server_s
 {
-  amcl_batch_t batch = nullptr;
+  struct Lane
+  {
+    amcl_batch_t batch = nullptr;
+    std::thread worker;
+    uint32_t sessions = 0;
+  };
+  std::vector<Lane> lanes;
+  uint64_t budget = 0, admitted = 0;  // particle capacity of the open sessions
   std::mutex mu;
   std::condition_variable cv;
   std::map<int64_t, Session> sessions;
   int64_t next_session = 1;
   uint64_t next_ticket = 1;
   std::vector<amcl_server_result> done;
-  std::thread worker;
   bool stop = false;
   int last_error = AMCL_OK;
   // statistics
@@ -70,8 +82,9 @@ struct amcl_server_s
 
 namespace
 {
-void worker_loop(amcl_server_s* S)
+void worker_loop(amcl_server_s* S, int lane)
 {
+  amcl_batch_t batch = S->lanes[lane].batch;
   struct InFlight
   {
     int64_t session;
@@ -93,7 +106,7 @@ void worker_loop(amcl_server_s* S)
           if (S->stop)
             return true;
           for (auto& kv : S->sessions)
-            if (!kv.second.pending.empty())
+            if (kv.second.lane == lane && !kv.second.pending.empty())
               return true;
           return false;
         });
@@ -102,10 +115,10 @@ void worker_loop(amcl_server_s* S)
       for (auto& kv : S->sessions)
       {
         Session& ss = kv.second;
-        if (ss.pending.empty())
+        if (ss.lane != lane || ss.pending.empty())
           continue;
         Request& r = ss.pending.front();
-        const int rc = amcl_batch_stage(S->batch, ss.slot, r.n ? r.xyz.data() : nullptr, r.n, 4,
+        const int rc = amcl_batch_stage(batch, ss.slot, r.n ? r.xyz.data() : nullptr, r.n, 4,
                                         r.nr ? r.ranges.data() : nullptr, r.nr, r.has_odom ? r.odom : nullptr,
                                         r.alpha, r.sigma, r.roll, r.pitch, r.resample);
         InFlight f{ kv.first, ss.slot, r.ticket, r.t_submit, 0 };
@@ -130,7 +143,7 @@ void worker_loop(amcl_server_s* S)
     // Wait for the step in flight, read its results, then launch the next one.
     if (!flight.empty())
     {
-      const int rc = amcl_batch_wait(S->batch);
+      const int rc = amcl_batch_wait(batch);
       const double t = now_s();
       std::lock_guard<std::mutex> lock(S->mu);
       S->busy_s += t - t_launch;
@@ -144,7 +157,7 @@ void worker_loop(amcl_server_s* S)
         res.t_done = t;
         float m7[7];
         double mv[8];
-        if (rc == AMCL_OK && amcl_batch_get_mean(S->batch, f.slot, m7, mv) == AMCL_OK)
+        if (rc == AMCL_OK && amcl_batch_get_mean(batch, f.slot, m7, mv) == AMCL_OK)
         {
           for (int k = 0; k < 4; ++k)
           {
@@ -164,7 +177,7 @@ void worker_loop(amcl_server_s* S)
     if (!next.empty())
     {
       t_launch = now_s();
-      const int rc = amcl_batch_step(S->batch);
+      const int rc = amcl_batch_step(batch);
       std::lock_guard<std::mutex> lock(S->mu);
       if (rc != AMCL_OK)
       {
@@ -191,21 +204,35 @@ void worker_loop(amcl_server_s* S)
 }
 }  // namespace
 
+extern "C" int amcl_server_create_lanes(amcl_server_t* out, uint32_t max_sessions, uint64_t max_particles,
+                                        uint64_t max_points_per_step, uint32_t lanes, void* stream)
+{
+  if (!out || !lanes || lanes > 16 || (stream && lanes != 1))
+    return amcl::fail(AMCL_EINVAL, "amcl_server_create_lanes: bad arguments (1-16 lanes; a caller's stream: 1 lane)");
+  amcl_server_s* S = new amcl_server_s();
+  S->budget = max_particles;
+  S->lanes.resize(lanes);
+  for (auto& L : S->lanes)
+  {
+    const int rc = amcl_batch_create(&L.batch, max_sessions, max_particles, max_points_per_step, stream);
+    if (rc)
+    {
+      for (auto& M : S->lanes)
+        amcl_batch_destroy(M.batch);
+      delete S;
+      return rc;
+    }
+  }
+  for (uint32_t k = 0; k < lanes; ++k)
+    S->lanes[k].worker = std::thread(worker_loop, S, static_cast<int>(k));
+  *out = S;
+  return AMCL_OK;
+}
+
 extern "C" int amcl_server_create(amcl_server_t* out, uint32_t max_sessions, uint64_t max_particles,
                                   uint64_t max_points_per_step, void* stream)
 {
-  if (!out)
-    return amcl::fail(AMCL_EINVAL, "amcl_server_create: null out");
-  amcl_server_s* S = new amcl_server_s();
-  const int rc = amcl_batch_create(&S->batch, max_sessions, max_particles, max_points_per_step, stream);
-  if (rc)
-  {
-    delete S;
-    return rc;
-  }
-  S->worker = std::thread(worker_loop, S);
-  *out = S;
-  return AMCL_OK;
+  return amcl_server_create_lanes(out, max_sessions, max_particles, max_points_per_step, stream ? 1u : 4u, stream);
 }
 
 extern "C" int amcl_server_destroy(amcl_server_t S)
@@ -219,9 +246,11 @@ extern "C" int amcl_server_destroy(amcl_server_t S)
       kv.second.pending.clear();
   }
   S->cv.notify_all();
-  if (S->worker.joinable())
-    S->worker.join();
-  amcl_batch_destroy(S->batch);
+  for (auto& L : S->lanes)
+    if (L.worker.joinable())
+      L.worker.join();
+  for (auto& L : S->lanes)
+    amcl_batch_destroy(L.batch);
   delete S;
   return AMCL_OK;
 }
@@ -229,22 +258,42 @@ extern "C" int amcl_server_destroy(amcl_server_t S)
 extern "C" int amcl_server_open_session(amcl_server_t S, amcl_grid_t grid, uint32_t capacity, uint64_t seed,
                                         int num_particles, const float init8[8], int64_t* session)
 {
-  if (!S || !grid || !init8 || !session)
+  if (!S || !grid || !init8 || !session || !capacity)
     return amcl::fail(AMCL_EINVAL, "amcl_server_open_session: bad arguments");
-  std::lock_guard<std::mutex> lock(S->mu);
+  const uint64_t need = (static_cast<uint64_t>(capacity) + 255) & ~255ull;
+  int lane = 0;
+  {
+    std::lock_guard<std::mutex> lock(S->mu);
+    if (S->admitted + need > S->budget)
+      return amcl::fail(AMCL_ENOMEM, "amcl_server_open_session: the particle budget is taken (admission refused)");
+    for (int k = 1; k < static_cast<int>(S->lanes.size()); ++k)
+      if (S->lanes[k].sessions < S->lanes[lane].sessions)
+        lane = k;
+    S->admitted += need;  // reserved while the slot is set up (without the server lock)
+    S->lanes[lane].sessions += 1;
+  }
+  amcl_batch_t batch = S->lanes[lane].batch;
   int slot = -1;
-  int rc = amcl_batch_add(S->batch, grid, capacity, seed, &slot);
-  if (rc)
-    return rc;  // AMCL_ENOMEM: no room in the arenas (admission refused)
-  rc = amcl_batch_init(S->batch, slot, num_particles, init8[0], init8[1], init8[2], init8[3], init8[4], init8[5],
-                       init8[6], init8[7]);
+  int rc = amcl_batch_add(batch, grid, capacity, seed, &slot);
+  if (!rc)
+  {
+    rc = amcl_batch_init(batch, slot, num_particles, init8[0], init8[1], init8[2], init8[3], init8[4], init8[5],
+                         init8[6], init8[7]);
+    if (rc)
+      amcl_batch_remove(batch, slot);
+  }
+  std::lock_guard<std::mutex> lock(S->mu);
   if (rc)
   {
-    amcl_batch_remove(S->batch, slot);
+    S->admitted -= need;
+    S->lanes[lane].sessions -= 1;
     return rc;
   }
   const int64_t id = S->next_session++;
-  S->sessions[id].slot = slot;
+  Session& ss = S->sessions[id];
+  ss.lane = lane;
+  ss.slot = slot;
+  ss.capacity = need;
   *session = id;
   return AMCL_OK;
 }
@@ -253,7 +302,10 @@ extern "C" int amcl_server_close_session(amcl_server_t S, int64_t session)
 {
   if (!S)
     return amcl::fail(AMCL_EINVAL, "amcl_server_close_session: null server");
-  // Wait until the session has nothing pending or in flight.
+  // Wait until the session has nothing pending or in flight, then take it out of the
+  // schedule and free its slot (waiting for the lane's current step, not under the
+  // server lock).
+  Session ss;
   for (int spins = 0;; ++spins)
   {
     {
@@ -263,15 +315,20 @@ extern "C" int amcl_server_close_session(amcl_server_t S, int64_t session)
         return amcl::fail(AMCL_EINVAL, "amcl_server_close_session: no such session");
       if (it->second.pending.empty() && it->second.in_flight == 0)
       {
-        const int rc = amcl_batch_remove(S->batch, it->second.slot);
+        ss = it->second;
         S->sessions.erase(it);
-        return rc;
+        break;
       }
     }
     if (spins > 200000)
       return amcl::fail(AMCL_ETIMEDOUT, "amcl_server_close_session: requests still pending");
     std::this_thread::sleep_for(std::chrono::microseconds(50));
   }
+  const int rc = amcl_batch_remove(S->lanes[ss.lane].batch, ss.slot);
+  std::lock_guard<std::mutex> lock(S->mu);
+  S->admitted -= ss.capacity;
+  S->lanes[ss.lane].sessions -= 1;
+  return rc;
 }
 
 extern "C" int amcl_server_submit(amcl_server_t S, int64_t session, const float* xyz, uint32_t n,
@@ -312,7 +369,7 @@ extern "C" int amcl_server_submit(amcl_server_t S, int64_t session, const float*
       *ticket = r.ticket;
     it->second.pending.push_back(std::move(r));
   }
-  S->cv.notify_one();
+  S->cv.notify_all();  // the session's lane picks it up
   return AMCL_OK;
 }
 
@@ -352,6 +409,6 @@ extern "C" int amcl_server_batch(amcl_server_t S, amcl_batch_t* batch)
 {
   if (!S || !batch)
     return amcl::fail(AMCL_EINVAL, "amcl_server_batch: bad arguments");
-  *batch = S->batch;
+  *batch = S->lanes[0].batch;
   return AMCL_OK;
 }

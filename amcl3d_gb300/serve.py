@@ -40,10 +40,10 @@ class ServerResult(C.Structure):
 
 
 class Server:
-    def __init__(self, max_sessions: int, max_particles: int, max_points_per_step: int):
+    def __init__(self, max_sessions: int, max_particles: int, max_points_per_step: int, lanes: int = 4):
         self._h = C.c_void_p()
-        N.call("amcl_server_create", C.byref(self._h), int(max_sessions), int(max_particles),
-               int(max_points_per_step), None)
+        N.call("amcl_server_create_lanes", C.byref(self._h), int(max_sessions), int(max_particles),
+               int(max_points_per_step), int(lanes), None)
         self._buf = (ServerResult * 4096)()
 
     def close(self):

@@ -584,7 +584,7 @@ def main():
     ap.add_argument("--rate", type=float, default=10.0, help="served config: requests/s per session")
     ap.add_argument("--duration", type=float, default=20.0, help="served config: measured seconds")
     ap.add_argument("--churn", type=float, default=5.0, help="served config: sessions joining/leaving per s")
-    ap.add_argument("--served-sessions", type=int, default=200,
+    ap.add_argument("--served-sessions", type=int, default=400,
                     help="sessions of the served-vs-plain section of the default line (0: skip)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))

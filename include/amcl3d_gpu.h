@@ -319,10 +319,10 @@ int amcl_batch_capacity(amcl_batch_t b, uint64_t* free_particles, uint32_t* free
 int amcl_batch_stream(amcl_batch_t b, void** stream);
 
 /* ---- server: many localisation sessions, continuous batching ------------------------------
- * No counterpart in the reference.  Sessions are filter slots of an internal batch
- * (state resident on the device); submitted update requests are served by a scheduler
- * thread that steps every session with a pending request together, staging requests
- * that arrive during a step for the next one.  Results come back through
+ * No counterpart in the reference.  Sessions are filter slots of internal batches
+ * (lanes; state resident on the device); submitted update requests are served by one
+ * scheduler thread per lane that steps every session of the lane with a pending
+ * request together, staging requests that arrive during a step for the next one.  Results come back through
  * amcl_server_poll in completion order; times are seconds of a monotonic clock. */
 typedef struct amcl_server_s* amcl_server_t;
 typedef struct
@@ -338,6 +338,11 @@ typedef struct
 
 int amcl_server_create(amcl_server_t* out, uint32_t max_sessions, uint64_t max_particles, uint64_t max_points_per_step,
                        void* stream);
+/* The same with `lanes` (1-16) concurrent batches, each with its own stream and
+ * scheduler thread (amcl_server_create: 4 lanes, or 1 on a caller's stream).  Every
+ * lane's arena can hold max_particles; max_particles bounds the sessions' total. */
+int amcl_server_create_lanes(amcl_server_t* out, uint32_t max_sessions, uint64_t max_particles,
+                             uint64_t max_points_per_step, uint32_t lanes, void* stream);
 int amcl_server_destroy(amcl_server_t s);
 /* Admission: AMCL_ENOMEM when the session does not fit in the remaining budget.
  * init8 = (x, y, z, yaw, x_dev, y_dev, z_dev, yaw_dev) of ParticleFilter::init. */
@@ -352,6 +357,7 @@ int amcl_server_submit(amcl_server_t s, int64_t session, const float* xyz, uint3
 int amcl_server_poll(amcl_server_t s, amcl_server_result* out, uint32_t cap, uint32_t* n);
 int amcl_server_stats(amcl_server_t s, uint64_t* steps, uint64_t* requests, double* busy_s, uint32_t* max_batch,
                       uint32_t* sessions);
+/* The batch of the first lane. */
 int amcl_server_batch(amcl_server_t s, amcl_batch_t* batch);
 
 /* Raw stream of the handle (cudaStream_t), for callers that time it with events. */
