@@ -29,11 +29,11 @@ using namespace amcl;
 
 namespace
 {
-constexpr int WT_THREADS = 256;
+constexpr int WT_THREADS = 192;  // 6 warps; 4 blocks per SM by registers (80 per thread)
 constexpr int WT_CHUNK = 1024;  // points staged per block iteration (16 KB)
 
 template <int STORAGE, int SUM>
-__global__ __launch_bounds__(WT_THREADS, 3) void k_weight_fused(WeightArgs a, GridView g)
+__global__ __launch_bounds__(WT_THREADS, 4) void k_weight_fused(WeightArgs a, GridView g)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   float4* s_pts = reinterpret_cast<float4*>(smem);

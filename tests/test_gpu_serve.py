@@ -1,5 +1,6 @@
 """Multi-session server (amcl_server_*): each session's results are identical to the
-same filter stepped alone (whatever else is in flight), admission refuses sessions
+same filter stepped alone (whatever else is in flight, on one lane or spread over
+concurrent lanes), admission refuses sessions
 beyond the budget, and host-side failures (unknown session, a session that leaves
 mid-stream, NaN inputs) stay contained."""
 
@@ -53,12 +54,13 @@ def drain(srv, n, timeout=60.0):
     return got
 
 
-def test_sessions_match_alone_in_the_mix(amcl, scene):
+@pytest.mark.parametrize("lanes", [1, 4])
+def test_sessions_match_alone_in_the_mix(amcl, scene, lanes):
     from amcl3d_gb300.serve import Server
 
     G, sessions = scene
     nreq = 3
-    srv = Server(max_sessions=8, max_particles=40000, max_points_per_step=10000)
+    srv = Server(max_sessions=8, max_particles=40000, max_points_per_step=10000, lanes=lanes)
     sids = []
     for sp in sessions:
         x, y, z, a = sp["pose"]
