@@ -217,7 +217,7 @@ def cpu_baseline(occ_points, info, scans, ranges, parts, seconds: float, threads
     }
 
 
-def reference_grid(occ_points, info, sample, scan, threads: int):
+def reference_grid(occ_points, info, sample, scan, threads: int, cell_limit: int = REF_CELL_LIMIT):
     """The grid the reference's CPU path reads, built on the host by the oracle's
     restatement of computeGrid: in full where the reference can build it itself, else
     (the warehouse's 1.6 G cells exceed its 250 M limit and would take hours on the
@@ -226,7 +226,7 @@ def reference_grid(occ_points, info, sample, scan, threads: int):
 
     size = tuple(int(v) for v in info["dims"])
     cells = int(np.prod(size))
-    if cells <= REF_CELL_LIMIT:
+    if cells <= cell_limit:
         d, p = O.compute_grid(occ_points, info["min"], info["max"], info["res"], 0.05, exp_mode=0, threads=threads)
         return O.GridData(info["min"], info["max"], info["res"], size, p.ravel(), d.ravel()), "full"
     prob = np.zeros(cells, np.float32)  # pages are mapped only where written
@@ -393,6 +393,7 @@ def run_ours(args, cfg, rank, world, local_rank):
         res["cpu_baseline"] = {"value": rate, "unit": UNIT, **desc}
     if rank == 0 and world == 1:
         res["voxel_filter"] = voxel_section(seed + 5)
+        res["grid_storage"] = storage_section(pf, G, parts, scans, ranges, odos, seed)
     if rank == 0 and world == 1 and args.served_sessions > 0:
         # p50/p99 update latency, served vs plain, on this GPU: sessions on this map and a room
         room = S.make_map(seed + 7, size_m=(20.0, 20.0, 5.0), n_boxes=40)
@@ -401,8 +402,90 @@ def run_ours(args, cfg, rank, world, local_rank):
         wh = S.make_map(seed, size_m=cfg["size_m"], res=0.05, n_boxes=cfg["n_boxes"], box_range=cfg["box_range"],
                         max_box_height=cfg["max_box_height"])
         del pf
+        res["batched"] = batched_section([G_room, G], [room, wh], seed + 9)
         res["served"] = served_vs_plain([G_room, G], [room, wh], args.served_sessions, 10.0, 8.0, 5.0)
     return res
+
+
+def storage_section(pf, G, parts, scans, ranges, odos, seed, steps=5):
+    """The same filter step with the grid's probabilities gathered as FP32, FP16 and
+    uint8 (amcl_grid_set_storage): cloud-weight kernel time and weights/s each."""
+    from amcl3d_gb300 import synth as S
+
+    out = {}
+    P = parts.shape[0]
+    for storage in ("f32", "f16", "u8"):
+        G.set_storage(storage)
+        pf.set_particles(parts)
+        pf.set_option(4, seed)
+        for k in range(2):
+            pf.predict(*S.ODOM_MODS, *odos[k % N_SCANS])
+            pf.update(G, scans[k % N_SCANS], ranges[k % N_SCANS], 0.5, 0.1, 0.0, 0.0)
+            pf.resample()
+        pf.profile(True)
+        pf.profile_read(reset=True)
+        weights = 0
+        for k in range(steps):
+            i = (2 + k) % N_SCANS
+            pf.predict(*S.ODOM_MODS, *odos[i])
+            pf.update(G, scans[i], ranges[i], 0.5, 0.1, 0.0, 0.0)
+            pf.getMean()
+            pf.resample()
+            weights += P * scans[i].shape[0]
+        prof = pf.profile_read(reset=True)
+        pf.profile(False)
+        ms, n = prof["cloud_weight"]
+        out[storage] = {"cloud_weight_ms": ms / n, "weights_per_s": weights / (ms / 1e3),
+                        "bytes_per_cell": {"f32": 4, "f16": 2, "u8": 1}[storage]}
+    G.set_storage("f32")
+    return out
+
+
+def batched_section(grids, maps, seed, n_filters=256, p_range=(1000, 200000), n_range=(500, 20000), steps=5):
+    """Many filters stepped together (amcl_batch_*): 256 filters, P log-uniform 1k-200k,
+    N log-uniform 500-20k, over the given maps; the batch autotuned once, then timed."""
+    from amcl3d_gb300 import serve as SV
+    from amcl3d_gb300 import synth as S
+    from amcl3d_gb300.batch import FilterBatch
+
+    rng = np.random.default_rng(seed)
+    pools = SV.make_scan_pool(maps, seed, n_range[1])
+    specs = []
+    for f in range(n_filters):
+        gi = int(rng.integers(len(grids)))
+        pose, scan, rg = pools[gi][int(rng.integers(len(pools[gi])))]
+        P = SV.log_uniform_int(rng, *p_range)
+        n = min(SV.log_uniform_int(rng, *n_range), scan.shape[0])
+        specs.append((gi, P, pose, scan[:n], rg))
+    B = FilterBatch(max_filters=n_filters, max_particles=sum(s[1] for s in specs) + 256 * n_filters,
+                    max_points_per_step=sum(s[3].shape[0] for s in specs))
+    slots = []
+    for f, (gi, P, pose, scan, rg) in enumerate(specs):
+        sl = B.add(grids[gi], P, seed * 1000 + f)
+        B.init(sl, P, pose[0], pose[1], pose[2], pose[3], 0.3, 0.3, 0.05, 0.1)
+        slots.append(sl)
+    odom = (*S.ODOM_MODS, 0.05, 0.0, 0.0, 0.01)
+
+    def step():
+        for sl, (gi, P, pose, scan, rg) in zip(slots, specs):
+            B.stage(sl, scan, rg, odom)
+        B.step()
+        B.wait()
+
+    step()
+    tuned = B.autotune(reps=2)
+    step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    dt = (time.perf_counter() - t0) / steps
+    weights = sum(P * scan.shape[0] for (gi, P, pose, scan, rg) in specs)
+    B.close()
+    return {"filters": n_filters, "particles": f"log-uniform {p_range}", "points": f"log-uniform {n_range}",
+            "particles_total": int(sum(s[1] for s in specs)), "weights_per_step": int(weights),
+            "ms_per_step": dt * 1e3, "weights_per_s": weights / dt,
+            "tuning": {"threads": tuned[0], "chunk": tuned[1]},
+            "timing": "host wall clock per step, scans staged from host memory each step"}
 
 
 def voxel_section(seed: int, leaf: float = 0.1, reps: int = 20):
