@@ -35,7 +35,7 @@ public:
    * or the GPU distance field (saved to the cache). */
   bool open(const std::string& map_path, const double sensor_dev);
 
-  /* North-star name of computeGrid: builds the field from already extracted
+  /* computeGrid under the name buildGridMap: builds the field from already extracted
    * occupied points and the octomap bounds. */
   bool buildGridMap(const pcl::PointCloud<pcl::PointXYZ>::Ptr& points, const double min[3], const double max[3],
                     const double resolution, const double sensor_dev);

@@ -75,7 +75,7 @@ int amcl_grid_create(amcl_grid_t* out, void* stream);
 int amcl_grid_destroy(amcl_grid_t g);
 
 /* computeGrid (PointCloudTools.cpp:84-149), reached through Grid3d::open
- * (Grid3d.cpp:25-78), spec alias buildGridMap: builds the nearest-occupied
+ * (Grid3d.cpp:25-78), also named buildGridMap: builds the nearest-occupied
  * squared-distance field and its probability c1*expf(-d2*d2*c2) on the device from
  * the occupied-leaf centres `xyz` (n points, `stride_floats` floats apart) and the
  * octomap bounds.  The reference refuses more than 250e6 cells
@@ -120,7 +120,7 @@ int amcl_grid_cloud_weights(amcl_grid_t g, const float* poses4, uint32_t P, cons
 
 /* No counterpart in the reference.  The same weights as amcl_grid_cloud_weights
  * for callers that must not allocate device memory (a real-time loop that may not
- * enter the driver's allocator, memory handed out only by a host framework's pool):
+ * enter the CUDA allocator, memory handed out only by a host framework's pool):
  * nothing is allocated; the two-phase kernel's scratch is a fixed 16 MiB
  * file-scope device array that every GPU loading the library holds until exit.
  * poses (P x float4 x, y, z, yaw) and cloud (n x float4 x, y, z, unused) are
@@ -161,7 +161,7 @@ int amcl_grid_slice(amcl_grid_t g, double z, int8_t* out, uint64_t cap, uint64_t
 int amcl_pf_create(amcl_pf_t* out, uint64_t seed, void* stream);
 int amcl_pf_destroy(amcl_pf_t pf);
 
-/* ParticleFilter::init (ParticleFilter.cpp:46-95), spec alias
+/* ParticleFilter::init (ParticleFilter.cpp:46-95), also named
  * buildParticlesPool: |num_particles| particles, particle 0 at the given pose, the
  * rest drawn from N(pose, dev) per axis; weights c1*exp(-d^2*c2) with
  * dev = max(x_dev, y_dev, z_dev), normalised; the mean is computed. */
