@@ -287,24 +287,81 @@ __global__ __launch_bounds__(256) void k_df_search(DFGeom gm, DFQuery q, const f
   float best[2] = { INFINITY, INFINITY };
   if (!__any_sync(0xFFFFFFFFu, valid[0] || valid[1]))
     return;
+  // This warp's cells span [qlo, qhi] per axis (corner coordinates ascend with the index).
+  const int x1 = min(bx * DF_B + DF_B, static_cast<int>(q.size[0])) - 1;
+  const int y1 = min(by * DF_B + DF_B, static_cast<int>(q.size[1])) - 1;
+  const float qlo[3] = { q.qx[bx * DF_B], q.qy[by * DF_B], qzv };
+  const float qhi[3] = { q.qx[x1], q.qy[y1], qzv };
+  const float bminf[3] = { static_cast<float>(gm.min[0]), static_cast<float>(gm.min[1]),
+                           static_cast<float>(gm.min[2]) };
+  const float bsizef = static_cast<float>(gm.bsize);
+  float worst = INFINITY;  // the largest best distance among the warp's cells, as of the last ring
   if (!q.empty)
   {
     const int rmax = max(gm.nb[0], max(gm.nb[1], gm.nb[2]));
     for (int r = 0; r <= rmax; ++r)
     {
-      const int side = 2 * r + 1;
-      const int ncube = side * side * side;
-      for (int base = 0; base < ncube; base += 32)
+      // The buckets at Chebyshev distance r form the surface of a (2r + 1)^3 cube:
+      // two z faces (2r + 1)^2, two y faces (2r + 1) x (2r - 1), two x faces (2r - 1)^2.
+      const int side = 2 * r + 1, inner = 2 * r - 1;
+      const int fz = side * side, fy = side * inner, fx = inner * inner;
+      const int nsurf = r == 0 ? 1 : 2 * (fz + fy + fx);
+      for (int base = 0; base < nsurf; base += 32)
       {
         const int li = base + lane;
         uint32_t s0 = 0, s1 = 0;
         bool have = false;
-        if (li < ncube)
+        if (li < nsurf)
         {
-          const int dx = li % side - r, dy = (li / side) % side - r, dz = li / (side * side) - r;
-          const int ch = max(abs(dx), max(abs(dy), abs(dz)));
+          int dx = 0, dy = 0, dz = 0;
+          if (r > 0)
+          {
+            int t = li;
+            if (t < 2 * fz)
+            {
+              dz = t < fz ? -r : r;
+              t %= fz;
+              dx = t % side - r;
+              dy = t / side - r;
+            }
+            else if ((t -= 2 * fz) < 2 * fy)
+            {
+              dy = t < fy ? -r : r;
+              t %= fy;
+              dx = t % side - r;
+              dz = t / side - (r - 1);
+            }
+            else
+            {
+              t -= 2 * fy;
+              dx = t < fx ? -r : r;
+              t %= fx;
+              dy = t % inner - (r - 1);
+              dz = t / inner - (r - 1);
+            }
+          }
           const int ux = bx + dx, uy = by + dy, uz = bz + dz;
-          if (ch == r && ux >= 0 && uy >= 0 && uz >= 0 && ux < gm.nb[0] && uy < gm.nb[1] && uz < gm.nb[2])
+          bool reach = ux >= 0 && uy >= 0 && uz >= 0 && ux < gm.nb[0] && uy < gm.nb[1] && uz < gm.nb[2];
+          if (reach && worst < INFINITY)
+          {
+            // Skip a bucket whose box is farther from every cell than each cell's best:
+            // per axis the gap between the cells' span and the bucket's box (edge buckets
+            // are open outward: clamped points lie there), less a slack far above the
+            // float rounding of the coordinates.
+            const int u[3] = { ux, uy, uz };
+            float d2 = 0.0f;
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+            {
+              const float blo = u[a] == 0 ? -INFINITY : bminf[a] + static_cast<float>(u[a]) * bsizef;
+              const float bhi = u[a] == gm.nb[a] - 1 ? INFINITY : bminf[a] + static_cast<float>(u[a] + 1) * bsizef;
+              const float slack = 1e-4f + 1e-6f * fmaxf(fabsf(qlo[a]), fabsf(qhi[a]));
+              const float gap = fmaxf(fmaxf(blo - qhi[a], qlo[a] - bhi) - slack, 0.0f);
+              d2 += gap * gap;
+            }
+            reach = !(d2 > worst * 1.00001f);
+          }
+          if (reach)
           {
             const uint64_t b = (static_cast<uint64_t>(uz) * gm.nb[1] + uy) * gm.nb[0] + ux;
             s0 = __ldg(start + b);
@@ -335,7 +392,7 @@ __global__ __launch_bounds__(256) void k_df_search(DFGeom gm, DFQuery q, const f
         }
       }
       // Unscanned buckets are >= r full buckets away from every cell of the brick.
-      float worst = fmaxf(valid[0] ? best[0] : 0.0f, valid[1] ? best[1] : 0.0f);
+      worst = fmaxf(valid[0] ? best[0] : 0.0f, valid[1] ? best[1] : 0.0f);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1)
         worst = fmaxf(worst, __shfl_xor_sync(0xFFFFFFFFu, worst, o));
