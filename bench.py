@@ -523,7 +523,7 @@ PLAIN_OPEN_MAX_SESSIONS = 400  # one plain filter (with its own weighting scratc
 
 
 def served_vs_plain(grids, maps, n_sessions, rate_hz, duration_s, churn_per_s, seed=7,
-                    p_range=(1000, 100000), n_range=(500, 10000), plain_requests=400):
+                    p_range=(1000, 100000), n_range=(500, 10000), plain_requests=400, max_queue=4):
     """Sessions served with continuous batching vs the same sessions each on its own
     plain filter (requests first come first served, one at a time) at the same offered
     load, on the same GPU; plus the plain path's closed-loop capacity.  Returns the
@@ -536,11 +536,13 @@ def served_vs_plain(grids, maps, n_sessions, rate_hz, duration_s, churn_per_s, s
                                                                         n_sessions * mean_p * 4)),
                     max_points_per_step=(n_sessions + 64) * n_range[1])
     t0 = time.perf_counter()
-    served = SV.run_load(srv, grids, pools, n_sessions, rate_hz, duration_s, churn_per_s, p_range, n_range, seed=seed)
+    served = SV.run_load(srv, grids, pools, n_sessions, rate_hz, duration_s, churn_per_s, p_range, n_range, seed=seed,
+                         max_queue=max_queue)
     log(f"served {n_sessions} sessions in {time.perf_counter() - t0:.1f}s: {served}")
     srv.close()
     if n_sessions <= PLAIN_OPEN_MAX_SESSIONS:
-        plain_open = SV.run_plain_open(grids, pools, n_sessions, rate_hz, duration_s, p_range, n_range, seed=seed)
+        plain_open = SV.run_plain_open(grids, pools, n_sessions, rate_hz, duration_s, p_range, n_range, seed=seed,
+                                       max_queue=max_queue)
         log(f"plain, same load: {plain_open}")
     else:
         plain_open = {"skipped": f"more than {PLAIN_OPEN_MAX_SESSIONS} plain filters (per-filter scratch)"}
@@ -549,6 +551,7 @@ def served_vs_plain(grids, maps, n_sessions, rate_hz, duration_s, churn_per_s, s
     return {
         "sessions": n_sessions, "rate_hz_per_session": rate_hz, "duration_s": duration_s,
         "churn_per_s": churn_per_s, "particles": f"log-uniform {p_range}", "points": f"log-uniform {n_range}",
+        "max_queued_scans_per_session": max_queue,
         "maps": [list(m.dims) for m in maps],
         "offered_weights_per_s": n_sessions * rate_hz * mean_p * (n_range[1] - n_range[0]) / math.log(
             n_range[1] / n_range[0]),
@@ -580,7 +583,7 @@ def run_served(args, rank, world, local_rank):
         m.occ = m.occ if m.dims[0] * m.dims[1] * m.dims[2] < 3e8 else m.occ  # kept for ray casting
         maps.append(m)
         grids.append(G)
-    res = served_vs_plain(grids, maps, args.sessions, args.rate, args.duration, args.churn)
+    res = served_vs_plain(grids, maps, args.sessions, args.rate, args.duration, args.churn, max_queue=args.max_queue)
     return {"metric": METRIC + " (served)", "value": res["weights_per_s"], "unit": UNIT, "n_gpus": world,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "config": {"workload": "served multi-session localization"}, "served": res}
@@ -667,6 +670,8 @@ def main():
     ap.add_argument("--rate", type=float, default=10.0, help="served config: requests/s per session")
     ap.add_argument("--duration", type=float, default=20.0, help="served config: measured seconds")
     ap.add_argument("--churn", type=float, default=5.0, help="served config: sessions joining/leaving per s")
+    ap.add_argument("--max-queue", type=int, default=4,
+                    help="served config: scans a session may have waiting; newer ones are skipped, as a busy node does")
     ap.add_argument("--served-sessions", type=int, default=400,
                     help="sessions of the served-vs-plain section of the default line (0: skip)")
     args = ap.parse_args()
