@@ -403,8 +403,62 @@ def run_ours(args, cfg, rank, world, local_rank):
                         max_box_height=cfg["max_box_height"])
         del pf
         res["batched"] = batched_section([G_room, G], [room, wh], seed + 9)
+        res["small_filters"] = small_filters_section(G_room, room, seed + 11)
         res["served"] = served_vs_plain([G_room, G], [room, wh], args.served_sessions, 10.0, 8.0, 5.0)
     return res
+
+
+def small_filters_section(G, m, seed, n_filters=512, P=1000, N=500, steps=5):
+    """Many small filters (1k particles, 500 points each, one room map): one batched
+    step for all of them against the plain path stepping them one call at a time."""
+    import amcl3d_gb300 as A
+    from amcl3d_gb300 import synth as S
+    from amcl3d_gb300.batch import FilterBatch
+
+    pose = S.free_pose(m, seed)
+    scan = S.ray_cast(m, pose, n_max=N, max_range=15.0, seed=seed + 1)
+    rg = S.beacons(m, pose, 3, seed=seed + 2)
+    odom = (*S.ODOM_MODS, 0.05, 0.0, 0.0, 0.01)
+    B = FilterBatch(max_filters=n_filters, max_particles=n_filters * (P + 256), max_points_per_step=n_filters * N)
+    slots = [B.add(G, P, seed * 1000 + f) for f in range(n_filters)]
+    for sl in slots:
+        B.init(sl, P, pose[0], pose[1], pose[2], pose[3], 0.3, 0.3, 0.05, 0.1)
+
+    def bstep():
+        for sl in slots:
+            B.stage(sl, scan, rg, odom)
+        B.step()
+        B.wait()
+
+    bstep()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        bstep()
+    batched_s = (time.perf_counter() - t0) / steps
+    B.close()
+    filters = [A.ParticleFilter(seed=seed * 1000 + f) for f in range(64)]
+    for pf in filters:
+        pf.init(P, pose[0], pose[1], pose[2], pose[3], 0.3, 0.3, 0.05, 0.1)
+
+    def pstep(pf):
+        pf.predict(*odom)
+        pf.update(G, scan, rg, 0.5, 0.1, 0.0, 0.0)
+        pf.getMean()
+        pf.resample()
+
+    for pf in filters:
+        pstep(pf)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for pf in filters:
+            pstep(pf)
+    plain_per_filter = (time.perf_counter() - t0) / (steps * len(filters))
+    w = P * scan.shape[0]
+    return {"filters": n_filters, "particles": P, "points": int(scan.shape[0]),
+            "batched_ms_per_step": batched_s * 1e3, "batched_weights_per_s": n_filters * w / batched_s,
+            "plain_ms_per_filter_step": plain_per_filter * 1e3, "plain_weights_per_s": w / plain_per_filter,
+            "batched_over_plain": (n_filters * w / batched_s) / (w / plain_per_filter),
+            "timing": "host wall clock; scans staged from host memory"}
 
 
 def storage_section(pf, G, parts, scans, ranges, odos, seed, steps=5):
