@@ -160,10 +160,23 @@ __global__ void __launch_bounds__(VX_THREADS) k_vx_hist(const uint32_t* __restri
   hist[threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
 }
 
-// Exclusive scan of L counters in place by one block; *total receives the sum.
-__global__ void __launch_bounds__(1024) k_vx_scan(uint32_t* __restrict__ a, uint32_t L, uint32_t* __restrict__ total)
+// Exclusive scan of L counters in place by one block; *total receives the sum.  With
+// STAGE the counters pass through shared memory (coalesced in and out; L <= VX_SCAN_SMEM).
+constexpr uint32_t VX_SCAN_SMEM = 24576;  // counters staged in 96 KB of shared memory
+
+template <bool STAGE>
+__global__ void __launch_bounds__(1024) k_vx_scan(uint32_t* __restrict__ ga, uint32_t L, uint32_t* __restrict__ total)
 {
+  extern __shared__ uint32_t s_a[];
   __shared__ uint32_t ws[32];
+  uint32_t* a = ga;
+  if (STAGE)
+  {
+    for (uint32_t i = threadIdx.x; i < L; i += 1024)
+      s_a[i] = ga[i];
+    __syncthreads();
+    a = s_a;
+  }
   const uint32_t per = (L + 1023) / 1024;
   const uint32_t lo = min(L, threadIdx.x * per), hi = min(L, lo + per);
   uint32_t s = 0;
@@ -204,6 +217,31 @@ __global__ void __launch_bounds__(1024) k_vx_scan(uint32_t* __restrict__ a, uint
   }
   if (threadIdx.x == 1023 && total)
     *total = run;
+  if (STAGE)
+  {
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < L; i += 1024)
+      ga[i] = s_a[i];
+  }
+}
+
+int launch_vx_scan(uint32_t* a, uint32_t L, uint32_t* total, cudaStream_t s)
+{
+  if (L <= VX_SCAN_SMEM)
+  {
+    static bool attr = false;
+    if (!attr)
+    {
+      AMCL_CUDA_TRY(cudaFuncSetAttribute(k_vx_scan<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(VX_SCAN_SMEM * 4)));
+      attr = true;
+    }
+    k_vx_scan<true><<<1, 1024, L * 4, s>>>(a, L, total);
+  }
+  else
+    k_vx_scan<false><<<1, 1024, 0, s>>>(a, L, total);
+  AMCL_LAUNCH_CHECK("k_vx_scan");
+  return AMCL_OK;
 }
 
 // Stable scatter of one tile by one digit.  Warp w owns the tile's keys
@@ -404,8 +442,8 @@ int voxel_enqueue(amcl_voxel_s* v, const float4* in, uint32_t n, const float lea
       const int shift = 8 * pass;
       k_vx_hist<<<ntiles, VX_THREADS, 0, s>>>(kA, n, shift, hist, ntiles);
       AMCL_LAUNCH_CHECK("k_vx_hist");
-      k_vx_scan<<<1, 1024, 0, s>>>(hist, 256u * ntiles, nullptr);
-      AMCL_LAUNCH_CHECK("k_vx_scan");
+      if ((rc = launch_vx_scan(hist, 256u * ntiles, nullptr, s)))
+        return rc;
       k_vx_scatter<<<ntiles, VX_THREADS, 0, s>>>(kA, vA, kB, vB, n, shift, hist, ntiles);
       AMCL_LAUNCH_CHECK("k_vx_scatter");
       std::swap(kA, kB);
@@ -414,8 +452,8 @@ int voxel_enqueue(amcl_voxel_s* v, const float4* in, uint32_t n, const float lea
     // after an even number of passes the sorted keys are back in keys[0] / vals[0]
     k_vx_heads<<<ntiles, VX_THREADS, 0, s>>>(kA, n, tiles, nullptr);
     AMCL_LAUNCH_CHECK("k_vx_heads");
-    k_vx_scan<<<1, 1024, 0, s>>>(tiles, ntiles, &meta->n_out);
-    AMCL_LAUNCH_CHECK("k_vx_scan");
+    if ((rc = launch_vx_scan(tiles, ntiles, &meta->n_out, s)))
+      return rc;
     k_vx_heads<<<ntiles, VX_THREADS, 0, s>>>(kA, n, tiles, starts);
     AMCL_LAUNCH_CHECK("k_vx_heads");
     k_vx_centroids<<<blocks_for(n, VX_THREADS, 1u << 30), VX_THREADS, 0, s>>>(in, n, vA, starts, meta, out);
