@@ -75,6 +75,32 @@ class FilterBatch:
                N.fptr(rg) if rg.size else None, rg.shape[0], N.dptr(od) if od is not None else None, float(alpha),
                float(sigma), float(roll), float(pitch), 1 if resample else 0)
 
+    def stage_many(self, slots, clouds, range_data=None, odom=None, alpha=0.5, sigma=0.1, roll=0.0, pitch=0.0,
+                   resample=True) -> None:
+        """stage() for many filters in one native call: clouds[k] (and range_data[k])
+        for slots[k]; odom is one (x_mod, y_mod, z_mod, a_mod, dx, dy, dz, da) for all,
+        a (count, 8) array, or None.  The clouds must share their stride (3 or 4 floats)."""
+        count = len(slots)
+        arrs = [_cloud_array(c) for c in clouds]
+        stride = arrs[0][1] if arrs else 4
+        if any(st != stride for _, st in arrs):
+            raise ValueError("stage_many: the clouds must all have the same stride")
+        rgs = [_ranges_array(r) for r in range_data] if range_data is not None else None
+        sl = np.ascontiguousarray(slots, dtype=np.int32)
+        ptrs = (C.c_void_p * count)(*[a.ctypes.data for a, _ in arrs])
+        ns = np.array([a.shape[0] for a, _ in arrs], dtype=np.uint32)
+        rptrs = (C.c_void_p * count)(*[r.ctypes.data if r.size else None for r in rgs]) if rgs else None
+        nrs = np.array([r.shape[0] for r in rgs], dtype=np.uint32) if rgs else None
+        od = None
+        if odom is not None:
+            o = np.asarray(odom, dtype=np.float64)
+            od = np.ascontiguousarray(np.broadcast_to(o, (count, 8)) if o.ndim == 1 else o.reshape(count, 8))
+        N.call("amcl_batch_stage_many", self._h, count, sl.ctypes.data_as(C.POINTER(C.c_int)), ptrs,
+               ns.ctypes.data_as(C.POINTER(C.c_uint32)), stride, rptrs,
+               nrs.ctypes.data_as(C.POINTER(C.c_uint32)) if nrs is not None else None,
+               N.dptr(od) if od is not None else None, float(alpha), float(sigma), float(roll), float(pitch),
+               1 if resample else 0)
+
     def step(self) -> None:
         N.call("amcl_batch_step", self._h)
 

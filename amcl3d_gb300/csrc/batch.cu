@@ -1295,15 +1295,17 @@ extern "C" int amcl_batch_get_particles(amcl_batch_t b, int slot, float* p7, uin
   return AMCL_OK;
 }
 
-extern "C" int amcl_batch_stage(amcl_batch_t b, int slot, const float* xyz, uint32_t n, uint32_t stride_floats,
-                                const float* ranges4, uint32_t nr, const double* odom8, double alpha, double sigma,
-                                double roll, double pitch, int resample)
+namespace
 {
-  if (!b || (n && !xyz) || (nr && !ranges4) || stride_floats < 3)
+// One filter's staged step (the batch lock held by the caller).
+int stage_locked(amcl_batch_s* b, int slot, const float* xyz, uint32_t n, uint32_t stride_floats,
+                 const float* ranges4, uint32_t nr, const double* odom8, double alpha, double sigma, double roll,
+                 double pitch, int resample)
+{
+  if ((n && !xyz) || (nr && !ranges4) || stride_floats < 3)
     return fail(AMCL_EINVAL, "amcl_batch_stage: bad arguments");
   if (nr > MAX_RANGES)
     return fail(AMCL_ERANGE, "amcl_batch_stage: more than 64 range measurements");
-  std::lock_guard<std::mutex> lock(b->mu);
   int rc = slot_check(b, slot);
   if (rc)
     return rc;
@@ -1324,6 +1326,36 @@ extern "C" int amcl_batch_stage(amcl_batch_t b, int slot, const float* xyz, uint
   sl.pitch = pitch;
   sl.resample = resample != 0;
   sl.staged = true;
+  return AMCL_OK;
+}
+}  // namespace
+
+extern "C" int amcl_batch_stage(amcl_batch_t b, int slot, const float* xyz, uint32_t n, uint32_t stride_floats,
+                                const float* ranges4, uint32_t nr, const double* odom8, double alpha, double sigma,
+                                double roll, double pitch, int resample)
+{
+  if (!b)
+    return fail(AMCL_EINVAL, "amcl_batch_stage: null batch");
+  std::lock_guard<std::mutex> lock(b->mu);
+  return stage_locked(b, slot, xyz, n, stride_floats, ranges4, nr, odom8, alpha, sigma, roll, pitch, resample);
+}
+
+extern "C" int amcl_batch_stage_many(amcl_batch_t b, uint32_t count, const int* slots, const float* const* clouds,
+                                     const uint32_t* n, uint32_t stride_floats, const float* const* ranges4,
+                                     const uint32_t* nr, const double* odom8, double alpha, double sigma, double roll,
+                                     double pitch, int resample)
+{
+  if (!b || (count && (!slots || !clouds || !n)))
+    return fail(AMCL_EINVAL, "amcl_batch_stage_many: bad arguments");
+  std::lock_guard<std::mutex> lock(b->mu);
+  for (uint32_t k = 0; k < count; ++k)
+  {
+    const uint32_t nrk = nr ? nr[k] : 0;
+    const int rc = stage_locked(b, slots[k], clouds[k], n[k], stride_floats, nrk && ranges4 ? ranges4[k] : nullptr,
+                                nrk, odom8 ? odom8 + 8ull * k : nullptr, alpha, sigma, roll, pitch, resample);
+    if (rc)
+      return rc;
+  }
   return AMCL_OK;
 }
 

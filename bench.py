@@ -429,8 +429,7 @@ def small_filters_section(G, m, seed, n_filters=512, P=1000, N=500, steps=5):
     def bstep():
         nonlocal t_stage, t_step
         t0 = time.perf_counter()
-        for sl in slots:
-            B.stage(sl, scan, rg, odom)
+        B.stage_many(slots, [scan] * len(slots), [rg] * len(slots), odom)
         t1 = time.perf_counter()
         B.step()
         B.wait()
@@ -468,8 +467,8 @@ def small_filters_section(G, m, seed, n_filters=512, P=1000, N=500, steps=5):
             "batched_over_plain_launch_and_wait": (n_filters * w / step_s) / (w / plain_per_filter),
             "plain_ms_per_filter_step": plain_per_filter * 1e3, "plain_weights_per_s": w / plain_per_filter,
             "batched_over_plain": (n_filters * w / batched_s) / (w / plain_per_filter),
-            "timing": "host wall clock; the batched step's scans are staged from Python one filter at a time "
-                      "(staging listed apart), the plain steps copy their scan inside update"}
+            "timing": "host wall clock; the batched step's scans are staged in one call (staging listed "
+                      "apart), the plain steps copy their scan inside update"}
 
 
 def storage_section(pf, G, parts, scans, ranges, odos, seed, steps=5):
@@ -531,9 +530,11 @@ def batched_section(grids, maps, seed, n_filters=256, p_range=(1000, 200000), n_
         slots.append(sl)
     odom = (*S.ODOM_MODS, 0.05, 0.0, 0.0, 0.01)
 
+    clouds = [sp[3] for sp in specs]
+    rgs = [sp[4] for sp in specs]
+
     def step():
-        for sl, (gi, P, pose, scan, rg) in zip(slots, specs):
-            B.stage(sl, scan, rg, odom)
+        B.stage_many(slots, clouds, rgs, odom)
         B.step()
         B.wait()
 

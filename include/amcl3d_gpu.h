@@ -293,6 +293,13 @@ int amcl_batch_get_particles(amcl_batch_t b, int slot, float* p7, uint32_t cap);
 int amcl_batch_stage(amcl_batch_t b, int slot, const float* xyz, uint32_t n, uint32_t stride_floats,
                      const float* ranges4, uint32_t nr, const double* odom8, double alpha, double sigma, double roll,
                      double pitch, int resample);
+/* amcl_batch_stage for `count` filters in one call: slots[k] gets clouds[k] (n[k]
+ * points, stride_floats apart), nr[k] ranges at ranges4[k] (nr and ranges4 may be
+ * NULL: no ranges), odometry odom8[8k..8k+7] (odom8 NULL: no predict); the other
+ * parameters are shared.  Stops at the first failing filter. */
+int amcl_batch_stage_many(amcl_batch_t b, uint32_t count, const int* slots, const float* const* clouds,
+                          const uint32_t* n, uint32_t stride_floats, const float* const* ranges4, const uint32_t* nr,
+                          const double* odom8, double alpha, double sigma, double roll, double pitch, int resample);
 /* Launches the staged steps of every filter (one CUDA graph launch); returns before
  * they finish.  Staging for the next step may proceed meanwhile. */
 int amcl_batch_step(amcl_batch_t b);

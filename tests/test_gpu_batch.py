@@ -128,3 +128,29 @@ def test_batch_admission(amcl, world):
     B.stage(b, big, None)
     with pytest.raises(N.AmclError):
         B.step()  # the staged clouds exceed max_points_per_step
+
+
+def test_stage_many_equals_stage(amcl, world):
+    """Staging every filter in one native call gives the same step as staging each."""
+    from amcl3d_gb300.batch import FilterBatch
+
+    grids, specs = world
+    out = []
+    for many in (False, True):
+        B = FilterBatch(max_filters=8, max_particles=40000, max_points_per_step=8000)
+        slots = [B.add(grids[sp["grid"]], sp["P"], sp["seed"]) for sp in specs]
+        for sl, sp in zip(slots, specs):
+            B.set_particles(sl, sp["parts"])
+        odom = (*MODS, 0.05, 0.01, 0.0, 0.02)
+        for s in range(2):
+            if many:
+                B.stage_many(slots, [sp["scans"][s] for sp in specs], [sp["ranges"] for sp in specs], odom)
+            else:
+                for sl, sp in zip(slots, specs):
+                    B.stage(sl, sp["scans"][s], sp["ranges"], odom)
+            B.step()
+            B.wait()
+        out.append([B.particles(sl, sp["P"]) for sl, sp in zip(slots, specs)])
+        B.close()
+    for a, b in zip(*out):
+        np.testing.assert_array_equal(a, b)
