@@ -259,39 +259,51 @@ struct DFQuery
   int empty;  // no occupied points at all
 };
 
-__global__ __launch_bounds__(256) void k_df_search(DFGeom gm, DFQuery q, const float4* __restrict__ pts,
-                                                   const uint32_t* __restrict__ start, float* __restrict__ dist,
-                                                   float* __restrict__ prob)
+constexpr int DF_LPW = 2;                         // z-layers of the brick per warp
+constexpr int DF_THREADS = 32 * DF_B / DF_LPW;    // warps per brick block
+constexpr int DF_NC = 2 * DF_LPW;                 // cells per lane
+
+__global__ __launch_bounds__(DF_THREADS) void k_df_search(DFGeom gm, DFQuery q, const float4* __restrict__ pts,
+                                                          const uint32_t* __restrict__ start, float* __restrict__ dist,
+                                                          float* __restrict__ prob)
 {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;  // wid = z-layer in brick
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const uint64_t brick = blockIdx.x;
   const int bx = static_cast<int>(brick % gm.nb[0]);
   const int by = static_cast<int>((brick / gm.nb[0]) % gm.nb[1]);
   const int bz = static_cast<int>(brick / (static_cast<uint64_t>(gm.nb[0]) * gm.nb[1]));
-  // two cells per lane: (lx, ly) = (lane & 7, lane >> 3) and (lane & 7, (lane >> 3) + 4)
-  int cx[2], cy[2];
-  const int cz = bz * DF_B + wid;
-  float qxv[2], qyv[2], qzv;
-  bool valid[2];
-  const bool zvalid = cz < static_cast<int>(q.size[2]);
-  qzv = zvalid ? q.qz[cz] : 0.0f;
+  // cells of this lane: x = lane & 7, y in {lane >> 3, (lane >> 3) + 4}, the warp's DF_LPW z-layers
+  const int cx = bx * DF_B + (lane & 7);
+  const int cy0 = by * DF_B + (lane >> 3);
+  int cy[DF_NC], cz[DF_NC];
+  float qxv, qyv[DF_NC], qzv[DF_NC];
+  bool valid[DF_NC];
+  bool any = false;
+  qxv = cx < static_cast<int>(q.size[0]) ? q.qx[cx] : 0.0f;
 #pragma unroll
-  for (int j = 0; j < 2; ++j)
+  for (int j = 0; j < DF_NC; ++j)
   {
-    cx[j] = bx * DF_B + (lane & 7);
-    cy[j] = by * DF_B + (lane >> 3) + 4 * j;
-    valid[j] = zvalid && cx[j] < static_cast<int>(q.size[0]) && cy[j] < static_cast<int>(q.size[1]);
-    qxv[j] = valid[j] ? q.qx[cx[j]] : 0.0f;
+    cy[j] = cy0 + 4 * (j & 1);
+    cz[j] = bz * DF_B + wid * DF_LPW + (j >> 1);
+    valid[j] = cx < static_cast<int>(q.size[0]) && cy[j] < static_cast<int>(q.size[1]) &&
+               cz[j] < static_cast<int>(q.size[2]);
     qyv[j] = valid[j] ? q.qy[cy[j]] : 0.0f;
+    qzv[j] = valid[j] ? q.qz[cz[j]] : 0.0f;
+    any |= valid[j];
   }
-  float best[2] = { INFINITY, INFINITY };
-  if (!__any_sync(0xFFFFFFFFu, valid[0] || valid[1]))
+  float best[DF_NC];
+#pragma unroll
+  for (int j = 0; j < DF_NC; ++j)
+    best[j] = INFINITY;
+  if (!__any_sync(0xFFFFFFFFu, any))
     return;
   // This warp's cells span [qlo, qhi] per axis (corner coordinates ascend with the index).
   const int x1 = min(bx * DF_B + DF_B, static_cast<int>(q.size[0])) - 1;
   const int y1 = min(by * DF_B + DF_B, static_cast<int>(q.size[1])) - 1;
-  const float qlo[3] = { q.qx[bx * DF_B], q.qy[by * DF_B], qzv };
-  const float qhi[3] = { q.qx[x1], q.qy[y1], qzv };
+  const int z0 = min(bz * DF_B + wid * DF_LPW, static_cast<int>(q.size[2]) - 1);
+  const int z1 = min(bz * DF_B + wid * DF_LPW + DF_LPW - 1, static_cast<int>(q.size[2]) - 1);
+  const float qlo[3] = { q.qx[bx * DF_B], q.qy[by * DF_B], q.qz[z0] };
+  const float qhi[3] = { q.qx[x1], q.qy[y1], q.qz[z1] };
   const float bminf[3] = { static_cast<float>(gm.min[0]), static_cast<float>(gm.min[1]),
                            static_cast<float>(gm.min[2]) };
   const float bsizef = static_cast<float>(gm.bsize);
@@ -379,20 +391,24 @@ __global__ __launch_bounds__(256) void k_df_search(DFGeom gm, DFQuery q, const f
           for (uint32_t i = a0; i < a1; ++i)
           {
             const float4 p = __ldg(pts + i);  // same address across the warp: broadcast
+            const float ddx = __fsub_rn(qxv, p.x);
+            const float dxx = __fmul_rn(ddx, ddx);
 #pragma unroll
-            for (int j = 0; j < 2; ++j)
+            for (int j = 0; j < DF_NC; ++j)
             {
-              const float ddx = __fsub_rn(qxv[j], p.x);
               const float ddy = __fsub_rn(qyv[j], p.y);
-              const float ddz = __fsub_rn(qzv, p.z);
-              const float d = __fadd_rn(__fadd_rn(__fmul_rn(ddx, ddx), __fmul_rn(ddy, ddy)), __fmul_rn(ddz, ddz));
+              const float ddz = __fsub_rn(qzv[j], p.z);
+              const float d = __fadd_rn(__fadd_rn(dxx, __fmul_rn(ddy, ddy)), __fmul_rn(ddz, ddz));
               best[j] = d < best[j] ? d : best[j];
             }
           }
         }
       }
       // Unscanned buckets are >= r full buckets away from every cell of the brick.
-      worst = fmaxf(valid[0] ? best[0] : 0.0f, valid[1] ? best[1] : 0.0f);
+      worst = 0.0f;
+#pragma unroll
+      for (int j = 0; j < DF_NC; ++j)
+        worst = fmaxf(worst, valid[j] ? best[j] : 0.0f);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1)
         worst = fmaxf(worst, __shfl_xor_sync(0xFFFFFFFFu, worst, o));
@@ -402,11 +418,11 @@ __global__ __launch_bounds__(256) void k_df_search(DFGeom gm, DFQuery q, const f
     }
   }
 #pragma unroll
-  for (int j = 0; j < 2; ++j)
+  for (int j = 0; j < DF_NC; ++j)
   {
     if (!valid[j])
       continue;
-    const uint64_t idx = (static_cast<uint64_t>(cz) * q.size[1] + cy[j]) * q.size[0] + cx[j];
+    const uint64_t idx = (static_cast<uint64_t>(cz[j]) * q.size[1] + cy[j]) * q.size[0] + cx;
     if (q.empty)
     {
       dist[idx] = -1.0f;  // PointCloudTools.cpp:142-143
@@ -606,7 +622,7 @@ extern "C" int amcl_grid_build(amcl_grid_t g, const float* xyz, uint64_t n, uint
   dq.c1 = static_cast<float>(1. / (sensor_dev * std::sqrt(2 * M_PI)));  // PointCloudTools.cpp:114
   dq.c2 = static_cast<float>(1. / (2. * sensor_dev * sensor_dev));      // PointCloudTools.cpp:115
   dq.empty = n == 0;
-  k_df_search<<<static_cast<unsigned>(gm.nbtot), 256, 0, s>>>(gm, dq, d_pts.as<float4>(), d_start.as<uint32_t>(),
+  k_df_search<<<static_cast<unsigned>(gm.nbtot), DF_THREADS, 0, s>>>(gm, dq, d_pts.as<float4>(), d_start.as<uint32_t>(),
                                                                 g->dist.as<float>(), g->prob.as<float>());
   AMCL_LAUNCH_CHECK("k_df_search");
   AMCL_CUDA_TRY(cudaStreamSynchronize(s));
