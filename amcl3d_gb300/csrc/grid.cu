@@ -145,12 +145,13 @@ void grid_apply_l2_window(amcl_grid_s* g, cudaStream_t s)
 // squared distance, accumulated in float as ((0 + dx*dx) + dy*dy) + dz*dz
 // (flann::L2_Simple over pcl::PointXYZ), plus prob = c1 * expf(-d2*d2*c2).
 //
-// Here: points are bucketed in cubes of DF_B^3 cells; one warp owns one z-layer of a
-// DF_B^3 brick (64 cells, two per lane) and scans the buckets in Chebyshev rings
-// around the brick with warp-uniform (broadcast) point loads, stopping once every
-// cell's best squared distance is below the squared distance to the first unscanned
-// ring.  The minimum of the same float expression over all points is exact: the
-// bound keeps a relative margin far above float rounding.
+// Here: points are bucketed in cubes of DF_B^3 cells; one warp owns DF_LPW z-layers of
+// a DF_B^3 brick (2 * DF_LPW cells per lane, sharing their x) and scans the buckets on
+// the surface of each Chebyshev ring around the brick with warp-uniform (broadcast)
+// point loads, skipping buckets whose box is farther from every cell than each cell's
+// best, and stopping once every cell's best squared distance is below the squared
+// distance to the first unscanned ring.  The minimum of the same float expression
+// over all points is exact: the bounds keep margins far above float rounding.
 
 namespace
 {
@@ -259,7 +260,7 @@ struct DFQuery
   int empty;  // no occupied points at all
 };
 
-constexpr int DF_LPW = 2;                         // z-layers of the brick per warp
+constexpr int DF_LPW = 4;                         // z-layers of the brick per warp
 constexpr int DF_THREADS = 32 * DF_B / DF_LPW;    // warps per brick block
 constexpr int DF_NC = 2 * DF_LPW;                 // cells per lane
 
