@@ -589,7 +589,7 @@ PLAIN_OPEN_MAX_SESSIONS = 400  # one plain filter (with its own weighting scratc
 
 
 def served_vs_plain(grids, maps, n_sessions, rate_hz, duration_s, churn_per_s, seed=7,
-                    p_range=(1000, 100000), n_range=(500, 10000), plain_requests=400, max_queue=4):
+                    p_range=(1000, 100000), n_range=(500, 10000), plain_requests=400, max_queue=4, lanes=4):
     """Sessions served with continuous batching vs the same sessions each on its own
     plain filter (requests first come first served, one at a time) at the same offered
     load, on the same GPU; plus the plain path's closed-loop capacity.  Returns the
@@ -600,7 +600,7 @@ def served_vs_plain(grids, maps, n_sessions, rate_hz, duration_s, churn_per_s, s
     mean_p = (p_range[1] - p_range[0]) / math.log(p_range[1] / p_range[0])
     srv = SV.Server(max_sessions=n_sessions + 64, max_particles=int(min(n_sessions * p_range[1],
                                                                         n_sessions * mean_p * 4)),
-                    max_points_per_step=(n_sessions + 64) * n_range[1])
+                    max_points_per_step=(n_sessions + 64) * n_range[1], lanes=lanes)
     t0 = time.perf_counter()
     served = SV.run_load(srv, grids, pools, n_sessions, rate_hz, duration_s, churn_per_s, p_range, n_range, seed=seed,
                          max_queue=max_queue)
@@ -617,7 +617,7 @@ def served_vs_plain(grids, maps, n_sessions, rate_hz, duration_s, churn_per_s, s
     return {
         "sessions": n_sessions, "rate_hz_per_session": rate_hz, "duration_s": duration_s,
         "churn_per_s": churn_per_s, "particles": f"log-uniform {p_range}", "points": f"log-uniform {n_range}",
-        "max_queued_scans_per_session": max_queue,
+        "max_queued_scans_per_session": max_queue, "lanes": lanes,
         "maps": [list(m.dims) for m in maps],
         "offered_weights_per_s": n_sessions * rate_hz * mean_p * (n_range[1] - n_range[0]) / math.log(
             n_range[1] / n_range[0]),
@@ -649,7 +649,8 @@ def run_served(args, rank, world, local_rank):
         m.occ = m.occ if m.dims[0] * m.dims[1] * m.dims[2] < 3e8 else m.occ  # kept for ray casting
         maps.append(m)
         grids.append(G)
-    res = served_vs_plain(grids, maps, args.sessions, args.rate, args.duration, args.churn, max_queue=args.max_queue)
+    res = served_vs_plain(grids, maps, args.sessions, args.rate, args.duration, args.churn, max_queue=args.max_queue,
+                          lanes=args.lanes)
     return {"metric": METRIC + " (served)", "value": res["weights_per_s"], "unit": UNIT, "n_gpus": world,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "config": {"workload": "served multi-session localization"}, "served": res}
@@ -736,6 +737,7 @@ def main():
     ap.add_argument("--rate", type=float, default=10.0, help="served config: requests/s per session")
     ap.add_argument("--duration", type=float, default=20.0, help="served config: measured seconds")
     ap.add_argument("--churn", type=float, default=5.0, help="served config: sessions joining/leaving per s")
+    ap.add_argument("--lanes", type=int, default=4, help="served config: concurrent server lanes")
     ap.add_argument("--max-queue", type=int, default=4,
                     help="served config: scans a session may have waiting; newer ones are skipped, as a busy node does")
     ap.add_argument("--served-sessions", type=int, default=400,
