@@ -3,7 +3,7 @@
 //
 // Some callers cannot call cudaMalloc at all: code running where the allocator is
 // owned by someone else (a real-time loop that must not page or block inside the
-// driver's allocator, a process whose device memory is handed out by a host
+// CUDA allocator, a process whose device memory is handed out by a host
 // framework's pool, code inside a memory budget that forbids new allocations).
 // This entry point computes the same per-particle cloud weights as
 // amcl_grid_cloud_weights with the two-phase kernel, but its scratch slab lives in
