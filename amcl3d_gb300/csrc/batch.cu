@@ -405,7 +405,7 @@ __global__ __launch_bounds__(NT) void k_b_blend(BatchDev d)
 __global__ __launch_bounds__(NT) void k_b_normalize(BatchDev d)
 {
   __shared__ double s_sum[2];
-  __shared__ X320 s_part[NT / 32];
+  __shared__ X320 s_part[NORM_Q * (NT / 32)];
   const uint32_t nitems = d.counts[1];
   for (uint32_t it = blockIdx.x; it < nitems; it += gridDim.x)
   {
@@ -418,14 +418,16 @@ __global__ __launch_bounds__(NT) void k_b_normalize(BatchDev d)
   }
 }
 
+// One warp per step.
 __global__ void k_b_finalize(BatchDev d)
 {
   const uint32_t n = d.counts[0];
-  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t s = warp; s < n; s += nwarps)
   {
     const SlotStep& st = d.steps[s];
     if (st.flags & ST_UPDATE)
-      finalize_stats(d.acc + static_cast<uint64_t>(st.slot) * ACC_WORDS, d.stats + st.slot);
+      finalize_stats_warp(d.acc + static_cast<uint64_t>(st.slot) * ACC_WORDS, d.stats + st.slot);
   }
 }
 
@@ -674,7 +676,7 @@ int enqueue_step(amcl_batch_s* b, int threads, int chunk, bool copies, uint32_t 
   AMCL_LAUNCH_CHECK("k_b_blend");
   k_b_normalize<<<grid, NT, 0, s>>>(d);
   AMCL_LAUNCH_CHECK("k_b_normalize");
-  k_b_finalize<<<1, 256, 0, s>>>(d);
+  k_b_finalize<<<static_cast<unsigned>(sms), 256, 0, s>>>(d);
   AMCL_LAUNCH_CHECK("k_b_finalize");
   k_b_prefix<<<grid, NT, 0, s>>>(d);
   AMCL_LAUNCH_CHECK("k_b_prefix");
@@ -1042,14 +1044,13 @@ __global__ __launch_bounds__(NT) void k_slot_normalize(uint32_t n, const float4*
                                                       unsigned long long* acc, X320* blocksum)
 {
   __shared__ double s_sum[2];
-  __shared__ X320 s_part[NT / 32];
+  __shared__ X320 s_part[NORM_Q * (NT / 32)];
   normalize_block(blockIdx.x, n, pose, w, acc, blocksum, s_sum, s_part);
 }
 
 __global__ void k_slot_finalize(const unsigned long long* acc, PFStats* st)
 {
-  if (threadIdx.x == 0 && blockIdx.x == 0)
-    finalize_stats(acc, st);
+  finalize_stats_warp(acc, st);  // one warp
 }
 }  // namespace
 

@@ -36,14 +36,13 @@ __global__ __launch_bounds__(NT) void k_normalize(uint32_t n, const float4* __re
                                                  unsigned long long* acc, X320* __restrict__ blocksum)
 {
   __shared__ double s_sum[2];
-  __shared__ X320 s_part[NT / 32];
+  __shared__ X320 s_part[NORM_Q * (NT / 32)];
   normalize_block(blockIdx.x, n, pose, w, acc, blocksum, s_sum, s_part);
 }
 
 __global__ void k_finalize_stats(const unsigned long long* acc, PFStats* st)
 {
-  if (threadIdx.x == 0 && blockIdx.x == 0)
-    finalize_stats(acc, st);
+  finalize_stats_warp(acc, st);  // one warp
 }
 
 __global__ __launch_bounds__(NT) void k_predict(float4* __restrict__ pose, PredictArgs a)

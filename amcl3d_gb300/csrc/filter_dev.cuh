@@ -93,10 +93,9 @@ __device__ __forceinline__ void blend_block(uint32_t blk, uint32_t n, const uint
 {
   __syncthreads();
   if (threadIdx.x == 0)
-  {
     s_sum[0] = acc_value(acc, ACC_WP);
+  if (threadIdx.x == 32)
     s_sum[1] = acc_value(acc, ACC_WR);
-  }
   __syncthreads();
   const double sp = s_sum[0], sr = s_sum[1];
   const uint32_t i = blk * NT + threadIdx.x;
@@ -116,10 +115,16 @@ __device__ __forceinline__ void blend_block(uint32_t blk, uint32_t n, const uint
 }
 
 // ---- normalise w, mean terms, per-block resample sums (ParticleFilter.cpp:182-195, :79-92) ----
+// Nine exact block sums (w, then w*c and w*c^2 per pose component c): each warp sums
+// them one after the other into s_part[quantity][warp] without a barrier, then one
+// barrier and the cross-warp sums run on separate warps.
+constexpr int NORM_Q = 9;
+
 __device__ __forceinline__ void normalize_block(uint32_t blk, uint32_t n, const float4* pose, float* w,
                                                 unsigned long long* acc, X320* blocksum, double* s_sum,
-                                                X320* s_part)
+                                                X320* s_part /* NORM_Q x (NT / 32) */)
 {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   __syncthreads();
   if (threadIdx.x == 0)
     s_sum[0] = acc_value(acc, ACC_W);
@@ -134,50 +139,74 @@ __device__ __forceinline__ void normalize_block(uint32_t blk, uint32_t n, const 
     w[i] = wv;
     p = pose[i];
   }
-  const X320 bs = block_exact_sum(x320_from_float(wv), s_part);
-  if (threadIdx.x == 0)
-  {
-    blocksum[blk] = bs;  // the resample prefix of this block
-    x320_atomic_add(acc + ACC_W2 * NDIG, bs);
-  }
+  X320 q = x320_warp_sum(x320_from_float(wv));
+  if (lane == 0)
+    s_part[wid] = q;
   const float c[4] = { p.x, p.y, p.z, p.w };
 #pragma unroll
   for (int k = 0; k < 4; ++k)
   {
     float hi, lo;
     two_prod(wv, c[k], hi, lo);
-    block_exact_add(x320_add(x320_from_float(hi), x320_from_float(lo)), acc + (ACC_M1 + k) * NDIG, s_part);
+    q = x320_warp_sum(x320_add(x320_from_float(hi), x320_from_float(lo)));
+    if (lane == 0)
+      s_part[(1 + k) * nw + wid] = q;
     // w*c^2 = w*(s + t) with c*c = s + t exactly; each product split again.
     float s, t, h1, l1, h2, l2;
     two_prod(c[k], c[k], s, t);
     two_prod(wv, s, h1, l1);
     two_prod(wv, t, h2, l2);
-    X320 q = x320_add(x320_add(x320_from_float(h1), x320_from_float(l1)),
-                      x320_add(x320_from_float(h2), x320_from_float(l2)));
-    block_exact_add(q, acc + (ACC_M2 + k) * NDIG, s_part);
+    q = x320_warp_sum(x320_add(x320_add(x320_from_float(h1), x320_from_float(l1)),
+                               x320_add(x320_from_float(h2), x320_from_float(l2))));
+    if (lane == 0)
+      s_part[(5 + k) * nw + wid] = q;
+  }
+  __syncthreads();
+  for (int j = wid; j < NORM_Q; j += nw)
+  {
+    X320 t = lane < nw ? s_part[j * nw + lane] : x320_zero();
+    t = x320_warp_sum(t);
+    if (lane == 0)
+    {
+      if (j == 0)
+      {
+        blocksum[blk] = t;  // the resample prefix of this block
+        x320_atomic_add(acc + ACC_W2 * NDIG, t);
+      }
+      else
+        x320_atomic_add(acc + (j <= 4 ? ACC_M1 + (j - 1) : ACC_M2 + (j - 5)) * NDIG, t);
+    }
   }
 }
 
-__device__ __forceinline__ void finalize_stats(const unsigned long long* acc, PFStats* st)
+// Sums, mean and variance from the exact accumulators, by one warp: lane k converts
+// accumulator k, lanes 0-3 finish pose component k.
+__device__ __forceinline__ void finalize_stats_warp(const unsigned long long* acc, PFStats* st)
 {
-  st->sum_wp = acc_value(acc, ACC_WP);
-  st->sum_wr = acc_value(acc, ACC_WR);
-  st->sum_w = acc_value(acc, ACC_W);
-  const double s2 = acc_value(acc, ACC_W2);
-  st->sum_w2 = s2;
-  for (int k = 0; k < 4; ++k)
+  const int lane = threadIdx.x & 31;
+  const double v = lane < ACC_COUNT ? acc_value(acc, lane) : 0.0;
+  const double s2 = __shfl_sync(0xFFFFFFFFu, v, ACC_W2);
+  const double m1 = __shfl_sync(0xFFFFFFFFu, v, ACC_M1 + (lane & 3));
+  const double m2 = __shfl_sync(0xFFFFFFFFu, v, ACC_M2 + (lane & 3));
+  if (lane == ACC_WP)
+    st->sum_wp = v;
+  if (lane == ACC_WR)
+    st->sum_wr = v;
+  if (lane == ACC_W)
+    st->sum_w = v;
+  if (lane == ACC_W2)
+    st->sum_w2 = v;
+  if (lane < 4)
   {
-    const double m1 = acc_value(acc, ACC_M1 + k);
-    const double m2 = acc_value(acc, ACC_M2 + k);
-    st->mean[k] = m1;  // the reference's mean is sum w*x of the normalised weights
-    st->mean_f[k] = __double2float_rn(m1);
+    st->mean[lane] = m1;  // the reference's mean is sum w*x of the normalised weights
+    st->mean_f[lane] = __double2float_rn(m1);
     if (s2 > 0)
     {
       const double mu = __ddiv_rn(m1, s2);
-      st->var[k] = __dsub_rn(__ddiv_rn(m2, s2), __dmul_rn(mu, mu));
+      st->var[lane] = __dsub_rn(__ddiv_rn(m2, s2), __dmul_rn(mu, mu));
     }
     else
-      st->var[k] = 0.0;
+      st->var[lane] = 0.0;
   }
 }
 
