@@ -354,13 +354,27 @@ def run_ours(args, cfg, rank, world, local_rank):
         step(k, resident=False)
     torch.cuda.synchronize()
     barrier(world)
-    t0 = time.perf_counter()
     e2e_weights = 0
-    for k in range(args.steps):
-        step(args.warmup + k, resident=False)
-        e2e_weights += P * scans[(args.warmup + k) % N_SCANS].shape[0]
-    torch.cuda.synchronize()
-    e2e_s = allreduce_max(time.perf_counter() - t0, world, dev)
+    if flush is None:
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            step(args.warmup + k, resident=False)
+            e2e_weights += P * scans[(args.warmup + k) % N_SCANS].shape[0]
+        torch.cuda.synchronize()
+        e2e_local = time.perf_counter() - t0
+    else:
+        # a grid that fits in L2: flush it before every step, each step timed on its own
+        e2e_local = 0.0
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_((k + 1) & 0xFF)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            step(args.warmup + k, resident=False)
+            torch.cuda.synchronize()
+            e2e_local += time.perf_counter() - t0
+            e2e_weights += P * scans[(args.warmup + k) % N_SCANS].shape[0]
+    e2e_s = allreduce_max(e2e_local, world, dev)
     e2e_total = allreduce_sum(e2e_weights, world, dev)
     h2d = int(np.mean([s.shape[0] for s in scans]) * 16 + cfg["B"] * 16)
     d2h = 4 + 120  # status word + the mean/variance record
