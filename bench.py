@@ -660,14 +660,17 @@ def run_served(args, rank, world, local_rank):
         m = S.make_map(300 + k, size_m=size, n_boxes=nb, max_box_height=hmax)
         G = A.Grid3d()
         G.buildGridMap(m.points, m.min, m.max, m.res, S.SENSOR_DEV)
-        m.occ = m.occ if m.dims[0] * m.dims[1] * m.dims[2] < 3e8 else m.occ  # kept for ray casting
+        if args.storage != "f32":
+            G.set_storage(args.storage)  # every session gathers from the narrower cells
         maps.append(m)
         grids.append(G)
     res = served_vs_plain(grids, maps, args.sessions, args.rate, args.duration, args.churn, max_queue=args.max_queue,
                           lanes=args.lanes)
     return {"metric": METRIC + " (served)", "value": res["weights_per_s"], "unit": UNIT, "n_gpus": world,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": {"workload": "served multi-session localization"}, "served": res}
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": {"f32": "f32", "f16": "f16 grid, f32 arithmetic", "u8": "u8 grid, f32 arithmetic"}[args.storage],
+            "data": "synthetic", "config": {"workload": "served multi-session localization", "grid_storage": args.storage},
+            "served": res}
 
 
 def run_reference(args, cfg, rank, world):
@@ -752,6 +755,7 @@ def main():
     ap.add_argument("--duration", type=float, default=20.0, help="served config: measured seconds")
     ap.add_argument("--churn", type=float, default=5.0, help="served config: sessions joining/leaving per s")
     ap.add_argument("--lanes", type=int, default=4, help="served config: concurrent server lanes")
+    ap.add_argument("--storage", choices=["f32", "f16", "u8"], default="f32", help="served config: grid storage")
     ap.add_argument("--max-queue", type=int, default=4,
                     help="served config: scans a session may have waiting; newer ones are skipped, as a busy node does")
     ap.add_argument("--served-sessions", type=int, default=400,
