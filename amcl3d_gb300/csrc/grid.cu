@@ -76,8 +76,16 @@ int grid_prepare_view(amcl_grid_s* g)
     const float U = float_ceil(octo_size);
     const float Tsz = g->tabs_host[off + in.size[a]];
     v.V[a] = std::min(U, Tsz);
-    v.inv_res[a] = static_cast<float>(1.0 / in.resolution);
-    v.eps[a] = static_cast<float>((static_cast<double>(in.size[a]) + 2.0) * std::ldexp(1.0, -22));
+    const double ir = 1.0 / in.resolution;
+    v.inv_res[a] = static_cast<float>(ir);
+    // 1/res is rounded by at most 2^-53 relative in ir; 2^-50 of room covers it
+    float lo = v.inv_res[a], hi = v.inv_res[a];
+    while (static_cast<double>(lo) > ir * (1.0 - std::ldexp(1.0, -50)))
+      lo = std::nextafter(lo, 0.0f);
+    while (static_cast<double>(hi) < ir * (1.0 + std::ldexp(1.0, -50)))
+      hi = std::nextafter(hi, INFINITY);
+    v.inv_lo[a] = lo;
+    v.inv_hi[a] = in.size[a] < (1u << 21) ? hi : INFINITY;
     v.min[a] = in.min[a];
     v.in_lo[a] = float_ceil(in.min[a]);
     v.in_hi[a] = float_ceil(in.max[a]);

@@ -51,7 +51,9 @@ struct GridView
   uint32_t toff[3];
   float V[3];
   float inv_res[3];
-  float eps[3];  // boundary margin of floor_near: (size + 2) * 2^-22
+  // 1/res bracketed by floats a little more than 2^-53 relative below and above it
+  // (inv_hi = +inf on an axis of 2^21 cells or more)
+  float inv_lo[3], inv_hi[3];
   double min[3];
   uint64_t cells;
   int built;
@@ -123,25 +125,23 @@ __device__ __forceinline__ int locate_pair(float X, const float2* T2, float V, f
   return (X < V) ? k : -1;
 }
 
-// Same result as locate_pair for an exact X, reading the table only near a cell
-// boundary.  q = fl32(X * fl32(1/res)) is within |q| * 2^-23 of X / res, and the
-// reference's floor(fl64(X / res)) differs from floor(X / res) only within 2^-53
-// relative of an integer; so when the fraction of q is at least eps =
-// (size + 2) * 2^-22 away from 0 and 1, floor(q) is the reference's cell.  Otherwise
-// (about 2 eps of the points per axis) the pair table settles it (near is set).
-// floor(q) without a float->int conversion: adding 1.5 * 2^23 rounded toward -inf
-// gives 1.5 * 2^23 + floor(q) exactly (the sum lies in [2^23, 2^24), where floats are
-// the integers), read off the sum's bit pattern; the fraction q - floor(q) is exact.
-// This holds for 0 <= q < 2^22: X >= 0 keeps q >= 0, X < V keeps q below size + 1,
-// and a size of 2^22 - 2 or more makes eps >= 1, sending every point to the table.
-// 1 - eps is exact (eps is a multiple of 2^-22).
-__device__ __forceinline__ int floor_near(float X, float inv_res, float eps, bool& near)
+// Same result as locate_pair for a valid X (0 <= X < V), reading the table only
+// near a cell boundary.  inv_lo <= 1/res <= inv_hi with more than 2^-53 relative
+// room on each side, and fl64 moves X / res by at most 2^-53 relative, so for X >= 0
+//   floor(X * inv_lo) <= floor(fl64(X / res)) <= floor(X * inv_hi);
+// when the two floors agree they are the reference's cell, otherwise (for about
+// X / res * 2^-22 of the points) `near` is set and the pair table settles it.  Each
+// floor is one fused multiply-add rounded toward -inf: X * inv + 1.5 * 2^23 lies in
+// [2^23, 2^24), where the floats are the integers, for 0 <= X * inv < 2^22, so the
+// rounded sum is 1.5 * 2^23 + floor(X * inv) exactly, read off its bit pattern.  A
+// valid X keeps X * inv_hi below size + 1 < 2^22; an axis of 2^21 cells or more has
+// inv_hi = +inf, which makes the floors disagree (or NaN) for every point.
+__device__ __forceinline__ int floor_bracket(float X, float inv_lo, float inv_hi, bool& near)
 {
-  const float q = fmul(X, inv_res);
-  const float r = __fadd_rd(q, 12582912.0f);
-  const float fr = fsub(q, fsub(r, 12582912.0f));
-  near |= (fr < eps) | (fr > 1.0f - eps);
-  return __float_as_int(r) - 0x4B400000;
+  const float lo = __fmaf_rd(X, inv_lo, 12582912.0f);
+  const float hi = __fmaf_rd(X, inv_hi, 12582912.0f);
+  near |= !(lo == hi);
+  return __float_as_int(lo) - 0x4B400000;
 }
 
 // True when a threshold lies within m of X (the estimate may then be on the wrong side).
@@ -218,12 +218,12 @@ __device__ __forceinline__ uint32_t cell_of_point(const GridView& g, const float
     for (int a = 0; a < 3; ++a)
     {
       X[a] = fadd(s[a], p.H[a]);
-      k[a] = floor_near(X[a], g.inv_res[a], g.eps[a], near);
+      k[a] = floor_bracket(X[a], g.inv_lo[a], g.inv_hi[a], near);
       // 0 <= X < V as one unsigned compare of the bit patterns: X is never -0.0 (H is
       // canonicalised), negative X and NaN have patterns above V's
       valid &= __float_as_uint(X[a]) < __float_as_uint(g.V[a]);
     }
-    if (near)
+    if (near && valid)
     {
 #pragma unroll
       for (int a = 0; a < 3; ++a)
