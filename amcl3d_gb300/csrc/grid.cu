@@ -91,6 +91,7 @@ int grid_prepare_view(amcl_grid_s* g)
     v.in_hi[a] = float_ceil(in.max[a]);
     off += in.size[a] + 1;
   }
+  v.neg_zero = -0.0f;
   v.step_y = in.size[0];
   v.step_z = in.size[0] * in.size[1];
   v.cells = g->cells();

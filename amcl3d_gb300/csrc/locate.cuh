@@ -54,6 +54,7 @@ struct GridView
   // 1/res bracketed by floats a little more than 2^-53 relative below and above it
   // (inv_hi = +inf on an axis of 2^21 cells or more)
   float inv_lo[3], inv_hi[3];
+  float neg_zero;  // -0.0f, read at run time (see PartYaw2)
   double min[3];
   uint64_t cells;
   int built;
@@ -187,6 +188,30 @@ enum : int
   XF_YAW = 2       // offsets are floats and roll = pitch = 0
 };
 
+// Cell index from exact coordinates X and their bracket floors k (floor_bracket),
+// 0xFFFFFFFF when the reference skips the point: the bound checks of
+// Grid3d.cpp:178-179 and 185 as 0 <= X < V, one unsigned compare of the bit
+// patterns per axis (X is never -0.0, H being canonicalised; negative X and NaN have
+// patterns above V's), and one branch for the rare point near a cell boundary.
+__device__ __forceinline__ uint32_t settle_cell(const GridView& g, const float2* tab, const float X[3], int k[3],
+                                                bool near)
+{
+  bool valid = true;
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+    valid &= __float_as_uint(X[a]) < __float_as_uint(g.V[a]);
+  if (near && valid)
+  {
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+      k[a] = locate_pair(X[a], tab + g.toff[a], g.V[a], g.inv_res[a], static_cast<int>(g.size[a]));
+    valid = (k[0] | k[1] | k[2]) >= 0;
+  }
+  if (!valid)
+    return 0xFFFFFFFFu;
+  return static_cast<uint32_t>(k[0]) + static_cast<uint32_t>(k[1]) * g.step_y + static_cast<uint32_t>(k[2]) * g.step_z;
+}
+
 // Grid cell of scan point (px, py, pz0) for the particle, 0xFFFFFFFF when the
 // reference skips it.  pz0 is s.z + 0.0f (Grid3d.cpp:174-176).  `tab` is the pair
 // table (in shared memory in the kernels).
@@ -210,29 +235,16 @@ __device__ __forceinline__ uint32_t cell_of_point(const GridView& g, const float
   int k[3];
   if (MODE != XF_GENERAL)
   {
-    // X = s + H exactly (float offsets); one branch per point for the rare
-    // near-boundary case, the bound checks of Grid3d.cpp:178-179 folded in.
+    // X = s + H exactly (float offsets)
     float X[3];
-    bool near = false, valid = true;
+    bool near = false;
 #pragma unroll
     for (int a = 0; a < 3; ++a)
     {
       X[a] = fadd(s[a], p.H[a]);
       k[a] = floor_bracket(X[a], g.inv_lo[a], g.inv_hi[a], near);
-      // 0 <= X < V as one unsigned compare of the bit patterns: X is never -0.0 (H is
-      // canonicalised), negative X and NaN have patterns above V's
-      valid &= __float_as_uint(X[a]) < __float_as_uint(g.V[a]);
     }
-    if (near && valid)
-    {
-#pragma unroll
-      for (int a = 0; a < 3; ++a)
-        k[a] = locate_pair(X[a], tab + g.toff[a], g.V[a], g.inv_res[a], static_cast<int>(g.size[a]));
-      valid = (k[0] | k[1] | k[2]) >= 0;
-    }
-    if (!valid)
-      return 0xFFFFFFFFu;
-    return static_cast<uint32_t>(k[0]) + static_cast<uint32_t>(k[1]) * g.step_y + static_cast<uint32_t>(k[2]) * g.step_z;
+    return settle_cell(g, tab, X, k, near);
   }
   bool amb = false;
 #pragma unroll
@@ -266,6 +278,58 @@ __device__ __forceinline__ float4 stage_point(float4 c, bool yaw_only)
   if (yaw_only && !(isfinite(c.x) && isfinite(c.y) && isfinite(c.z)))
     c.x = __int_as_float(0x7FC00000);
   return c;
+}
+
+// The yaw-only transform with the x and y axes paired in the two-wide float
+// instructions of sm_100 and later (each half rounds as the scalar instruction): the
+// same operations as cell_of_point<XF_YAW> in fewer issues.  The scan point is
+// staged as (x, x, y, y) so that both products of a coordinate come from one register
+// pair.  The reference rounds the two products and their sum separately, but the
+// code generator contracts a two-wide multiply feeding a two-wide add into a fused
+// multiply-add even when both carry an explicit round-to-nearest; so each product is
+// a fused multiply-add with an addend of -0.0 that the compiler cannot see as a
+// constant (GridView::neg_zero, a kernel argument).  fma(a, b, -0) is the rounded
+// product a * b for every input, signed zeros included, and nothing contracts a
+// fused multiply-add into a following add.
+struct PartYaw2
+{
+  float2 rx, ry;  // (r00, r10), (r01, r11)
+  float2 h;       // (H_x, H_y)
+  float2 lo, hi;  // (inv_lo, inv_hi) of the x and y axes
+  float2 nz;      // (-0.0, -0.0), opaque to the compiler
+  float hz, loz, hiz;
+};
+
+__device__ __forceinline__ PartYaw2 pair_yaw(const GridView& g, const PartXf& p)
+{
+  PartYaw2 q;
+  q.rx = make_float2(p.r[0], p.r[3]);
+  q.ry = make_float2(p.r[1], p.r[4]);
+  q.h = make_float2(p.H[0], p.H[1]);
+  q.lo = make_float2(g.inv_lo[0], g.inv_lo[1]);
+  q.hi = make_float2(g.inv_hi[0], g.inv_hi[1]);
+  q.nz = make_float2(g.neg_zero, g.neg_zero);
+  q.hz = p.H[2];
+  q.loz = g.inv_lo[2];
+  q.hiz = g.inv_hi[2];
+  return q;
+}
+
+__device__ __forceinline__ uint32_t cell_of_point_yaw2(const GridView& g, const float2* tab, const PartYaw2& q,
+                                                       float4 xxyy, float pz0)
+{
+  const float2 s01 = __fadd2_rn(__ffma2_rn(make_float2(xxyy.x, xxyy.y), q.rx, q.nz),
+                                __ffma2_rn(make_float2(xxyy.z, xxyy.w), q.ry, q.nz));
+  const float2 X01 = __fadd2_rn(s01, q.h);
+  const float2 c2 = make_float2(12582912.0f, 12582912.0f);
+  const float2 lo = __ffma2_rd(X01, q.lo, c2), hi = __ffma2_rd(X01, q.hi, c2);
+  const float Xz = fadd(pz0, q.hz);
+  const float loz = __fmaf_rd(Xz, q.loz, 12582912.0f), hiz = __fmaf_rd(Xz, q.hiz, 12582912.0f);
+  const bool near = !(lo.x == hi.x) | !(lo.y == hi.y) | !(loz == hiz);
+  const float X[3] = { X01.x, X01.y, Xz };
+  int k[3] = { __float_as_int(lo.x) - 0x4B400000, __float_as_int(lo.y) - 0x4B400000,
+               __float_as_int(loz) - 0x4B400000 };
+  return settle_cell(g, tab, X, k, near);
 }
 
 template <int STORAGE>

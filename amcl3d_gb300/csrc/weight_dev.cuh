@@ -7,7 +7,8 @@
 
 namespace amcl
 {
-constexpr int UNROLL = 4;
+constexpr int UNROLL = 8;
+constexpr int YAW_UNROLL = 8;  // points per group of the paired yaw-only loop
 constexpr int MAX_RANGES = 64;
 
 __device__ __forceinline__ float exp_f32_via_f64(float x) { return __double2float_rn(exp(static_cast<double>(x))); }
@@ -60,10 +61,11 @@ struct CloudSum
 };
 
 // Adds the points [0, cnt) of a staged chunk (cnt a multiple of UNROLL, padding
-// points NaN) in order.
-template <int STORAGE, int SUM, int MODE>
-__device__ __forceinline__ void weigh_chunk(const float4* s_pts, uint32_t cnt, const float2* s_tab, const GridView& g,
-                                            const PartXf& xf, CloudSum<SUM>& acc)
+// points NaN) in order.  Points are float4 (x, y, z + 0, -), or with YL the
+// yaw-only staging: (x, x, y, y) in s_pts and z + 0 in s_z.
+template <int STORAGE, int SUM, int MODE, bool YL>
+__device__ __forceinline__ void weigh_chunk(const float4* s_pts, const float* s_z, uint32_t cnt, const float2* s_tab,
+                                            const GridView& g, const PartXf& xf, CloudSum<SUM>& acc)
 {
   for (uint32_t k = 0; k < cnt; k += UNROLL)
   {
@@ -72,7 +74,8 @@ __device__ __forceinline__ void weigh_chunk(const float4* s_pts, uint32_t cnt, c
     for (int j = 0; j < UNROLL; ++j)
     {
       const float4 s = s_pts[k + j];
-      cell[j] = cell_of_point<MODE>(g, s_tab, xf, s.x, s.y, s.z);
+      cell[j] = YL ? cell_of_point<MODE>(g, s_tab, xf, s.x, s.z, s_z[k + j])
+                   : cell_of_point<MODE>(g, s_tab, xf, s.x, s.y, s.z);
     }
     float v[UNROLL];
 #pragma unroll
@@ -80,6 +83,41 @@ __device__ __forceinline__ void weigh_chunk(const float4* s_pts, uint32_t cnt, c
       v[j] = cell[j] != 0xFFFFFFFFu ? gather_prob<STORAGE>(g, cell[j]) : 0.0f;
 #pragma unroll
     for (int j = 0; j < UNROLL; ++j)
+      if (cell[j] != 0xFFFFFFFFu)
+        acc.add(v[j]);
+  }
+}
+
+// weigh_chunk of the yaw-only mode on the yaw-only staging, x and y paired, YAW_UNROLL
+// points per group (cnt a multiple of it).
+template <int STORAGE, int SUM>
+__device__ __forceinline__ void weigh_chunk_yaw2(const float4* s_pts, const float* s_z, uint32_t cnt,
+                                                 const float2* s_tab, const GridView& g, const PartYaw2& q,
+                                                 CloudSum<SUM>& acc)
+{
+  static_assert(YAW_UNROLL % 4 == 0, "z is read a float4 at a time");
+  for (uint32_t k = 0; k < cnt; k += YAW_UNROLL)
+  {
+    float zs[YAW_UNROLL];
+#pragma unroll
+    for (int j = 0; j < YAW_UNROLL; j += 4)
+    {
+      const float4 z4 = *reinterpret_cast<const float4*>(s_z + k + j);
+      zs[j] = z4.x;
+      zs[j + 1] = z4.y;
+      zs[j + 2] = z4.z;
+      zs[j + 3] = z4.w;
+    }
+    uint32_t cell[YAW_UNROLL];
+#pragma unroll
+    for (int j = 0; j < YAW_UNROLL; ++j)
+      cell[j] = cell_of_point_yaw2(g, s_tab, q, s_pts[k + j], zs[j]);
+    float v[YAW_UNROLL];
+#pragma unroll
+    for (int j = 0; j < YAW_UNROLL; ++j)
+      v[j] = cell[j] != 0xFFFFFFFFu ? gather_prob<STORAGE>(g, cell[j]) : 0.0f;
+#pragma unroll
+    for (int j = 0; j < YAW_UNROLL; ++j)
       if (cell[j] != 0xFFFFFFFFu)
         acc.add(v[j]);
   }
@@ -185,8 +223,9 @@ __device__ __forceinline__ void load_tables(const GridView& g, float2* s_tab)
 
 // One block of particles [p0, p0 + blockDim) of one filter, one thread per particle
 // over the whole cloud in cloud order (the fused weighting).  The caller has loaded
-// s_tab (when a.N > 0) and s_rg.  Points are staged `chunk` at a time (a multiple of
-// UNROLL).  Every thread of the block must call this.
+// s_tab (when a.N > 0) and s_rg.  s_pts holds `chunk` float4 (a multiple of UNROLL):
+// as many points per stage, or 4/5 as many (a multiple of YAW_UNROLL) in the yaw-only
+// staging.  Every thread of the block must call this.
 template <int STORAGE, int SUM>
 __device__ __forceinline__ void weigh_block(const WeightArgs& a, const GridView& g, uint32_t p0, uint32_t chunk,
                                             float4* s_pts, const float4* s_rg, X320* s_part, const float2* s_tab)
@@ -205,26 +244,47 @@ __device__ __forceinline__ void weigh_block(const WeightArgs& a, const GridView&
   const bool warp_exact = __all_sync(0xFFFFFFFFu, xf.exact != 0);
   const int mode = warp_exact ? (a.yaw_only ? XF_YAW : XF_EXACT) : XF_GENERAL;
 
+  // Yaw-only filters stage (x, x, y, y) and z separately: 20 B per point, so a
+  // chunk holds 4/5 as many points in the same shared memory.
+  const bool yl = a.yaw_only != 0;
+  const uint32_t al = yl ? YAW_UNROLL : UNROLL;  // padding of a staged chunk (NaN points)
+  const uint32_t ch = yl ? (chunk * 4 / 5) / al * al : chunk;
+  float* s_z = reinterpret_cast<float*>(s_pts + ch);
+  PartYaw2 q{};
+  if (inm && mode == XF_YAW)
+    q = pair_yaw(g, xf);
+
   CloudSum<SUM> acc;
-  for (uint32_t base = 0; base < a.N; base += chunk)
+  for (uint32_t base = 0; base < a.N; base += ch)
   {
-    const uint32_t cnt = min(chunk, a.N - base);
-    const uint32_t cnt8 = (cnt + UNROLL - 1) / UNROLL * UNROLL;
+    const uint32_t cnt = min(ch, a.N - base);
+    const uint32_t cnt8 = (cnt + al - 1) / al * al;
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < cnt8; i += blockDim.x)
     {
       const float nan = __int_as_float(0x7FC00000);
-      s_pts[i] = i < cnt ? stage_point(a.cloud[base + i], a.yaw_only != 0) : make_float4(nan, nan, nan, 0.0f);
+      const float4 c = i < cnt ? stage_point(a.cloud[base + i], yl) : make_float4(nan, nan, nan, 0.0f);
+      if (yl)
+      {
+        s_pts[i] = make_float4(c.x, c.x, c.y, c.y);
+        s_z[i] = c.z;
+      }
+      else
+      {
+        s_pts[i] = c;
+      }
     }
     __syncthreads();
     if (!inm)
       continue;
     if (mode == XF_YAW)
-      weigh_chunk<STORAGE, SUM, XF_YAW>(s_pts, cnt8, s_tab, g, xf, acc);
+      weigh_chunk_yaw2<STORAGE, SUM>(s_pts, s_z, cnt8, s_tab, g, q, acc);
     else if (mode == XF_EXACT)
-      weigh_chunk<STORAGE, SUM, XF_EXACT>(s_pts, cnt8, s_tab, g, xf, acc);
+      weigh_chunk<STORAGE, SUM, XF_EXACT, false>(s_pts, s_z, cnt8, s_tab, g, xf, acc);
+    else if (yl)
+      weigh_chunk<STORAGE, SUM, XF_GENERAL, true>(s_pts, s_z, cnt8, s_tab, g, xf, acc);
     else
-      weigh_chunk<STORAGE, SUM, XF_GENERAL>(s_pts, cnt8, s_tab, g, xf, acc);
+      weigh_chunk<STORAGE, SUM, XF_GENERAL, false>(s_pts, s_z, cnt8, s_tab, g, xf, acc);
   }
   float wpv = 0.0f, wrv = 0.0f;
   if (inm)

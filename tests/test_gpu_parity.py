@@ -175,6 +175,25 @@ def test_cloud_weights_on_lattice_boundaries(amcl, small):
     np.testing.assert_array_equal(w_gpu, w_orc)
 
 
+@pytest.mark.parametrize("roll,pitch", [(0.0, 0.0), (0.01, -0.02)])
+def test_cloud_weights_one_thread_per_particle(amcl, roll, pitch):
+    """Enough particles for the one-thread-per-particle weighting (65,536) on a map whose
+    minimum is 0, so every offset is an exact float: the yaw-only path (x and y paired
+    in two-wide instructions) and the exact-offset path, against the oracle.  About one
+    pair in a million has a transformed coordinate within an ulp of a cell boundary,
+    where an extra rounding step (or a missing one) moves the point to the next cell."""
+    m = S.make_map(32, size_m=(10.0, 10.0, 4.0), n_boxes=12)
+    G = amcl.Grid3d()
+    assert G.buildGridMap(m.points, m.min, m.max, m.res, S.SENSOR_DEV)
+    pose = S.free_pose(m, 43, height=1.2, clearance=0.4)
+    scan = S.ray_cast(m, pose, n_max=1200, max_range=8.0, seed=53)
+    poses = np.ascontiguousarray(S.particles_around(pose, 65536, 63)[:, :4])
+    w_gpu = G.computeCloudWeights(poses, scan, roll, pitch)
+    inf = G.info()
+    g = O.GridData(inf["min"], inf["max"], inf["resolution"], inf["size"], G.read_cells()[1])
+    np.testing.assert_array_equal(w_gpu, O.cloud_weights(g, poses, scan, roll, pitch, yaw_trig=1))
+
+
 # ---- update / normalise / mean --------------------------------------------------------------------
 
 def run_update(amcl, G, parts, scan, ranges, alpha=0.5, sigma=0.1, roll=0.0, pitch=0.0, kernel=0, cloud_sum=0):
