@@ -64,7 +64,18 @@ struct SlotStep
   double alpha;
   PredictArgs pred;
   float factor, r;
+  int32_t gslot;  // index of g in the launch's GridSet, -1: read g from here
   GridView g;
+};
+
+// The grids of a batch passed by value to the fused weighting launches: a step whose
+// grid is in the set reads the grid's fields (bounds, strides, cell array) from the
+// kernel's constant bank, as the single-filter kernel does, rather than holding them
+// in registers after a load from the step descriptor.
+constexpr int BATCH_GRIDS = 4;
+struct GridSet
+{
+  GridView g[BATCH_GRIDS];
 };
 
 // Per-particle transform of a split step (computed once per step).
@@ -115,8 +126,9 @@ __global__ __launch_bounds__(NT) void k_b_predict(BatchDev d)
 }
 
 template <int STORAGE, int SUM>
-__device__ __forceinline__ void b_weigh(const BatchDev& d, const SlotStep& st, uint32_t tile, uint32_t chunk,
-                                        float4* s_pts, const float4* s_rg, X320* s_part, const float2* s_tab)
+__device__ __forceinline__ void b_weigh(const BatchDev& d, const SlotStep& st, const GridView& g, uint32_t tile,
+                                        uint32_t chunk, float4* s_pts, const float4* s_rg, X320* s_part,
+                                        const float2* s_tab)
 {
   WeightArgs a{};
   a.pose = d.pose[st.cur] + st.p_off;
@@ -136,19 +148,31 @@ __device__ __forceinline__ void b_weigh(const BatchDev& d, const SlotStep& st, u
   a.acc_wp = d.acc + static_cast<uint64_t>(st.slot) * ACC_WORDS + ACC_WP * NDIG;
   a.acc_wr = d.acc + static_cast<uint64_t>(st.slot) * ACC_WORDS + ACC_WR * NDIG;
   a.yaw_only = st.yaw_only;
-  weigh_block<STORAGE, SUM>(a, st.g, tile * blockDim.x, chunk, s_pts, s_rg, s_part, s_tab);
+  weigh_block<STORAGE, SUM>(a, g, tile * blockDim.x, chunk, s_pts, s_rg, s_part, s_tab);
 }
 
-// Persistent: blocks take (filter, particle tile) items of one (storage, sum) class
-// until that class's queue is empty.
-constexpr int N_CLASSES = 6;  // 3 storages x 2 sum modes
-// counts: [0] steps, [1] block items, [2] weight items, [4 + 2c, 5 + 2c) fused class
-// c's items, [16 + 2c, 17 + 2c) split class c's items
-constexpr int COUNT_WORDS = 32;
+// Persistent: blocks take (filter, particle tile) items of one fused queue until it is
+// empty.  A fused queue holds the items of one (storage, sum) class on one grid slot:
+// slots 0..BATCH_GRIDS-1 are launched with their grid as a kernel argument (its fields
+// read from the constant bank: fewer registers, three 256-thread blocks per SM), the
+// last slot reads each step's grid from its descriptor.
+constexpr int N_CLASSES = 6;                         // 3 storages x 2 sum modes
+constexpr int N_GSLOTS = BATCH_GRIDS + 1;            // grid slots + the descriptor path
+constexpr int N_FUSED_Q = N_CLASSES * N_GSLOTS;      // fused queues
+constexpr int N_COUNTERS = N_FUSED_Q + N_CLASSES;    // fused queues, then split classes
+constexpr int SPLIT_MASK_SHIFT = 32;                 // class mask: bit q fused queue q, bit 32 + c split class c
+static_assert(N_FUSED_Q <= SPLIT_MASK_SHIFT, "fused queues fit below the split bits");
+// counts: [0] steps, [1] block items, [2] weight items, [FQ_BASE + 2q, FQ_BASE + 2q + 1)
+// fused queue q's items, [SQ_BASE + 2c, SQ_BASE + 2c + 1) split class c's items
+constexpr int FQ_BASE = 4;
+constexpr int SQ_BASE = FQ_BASE + 2 * N_FUSED_Q;
+constexpr int COUNT_WORDS = SQ_BASE + 2 * N_CLASSES;
 __host__ __device__ inline int weight_class(int storage, int cloud_sum) { return storage * 2 + (cloud_sum ? 1 : 0); }
+__host__ __device__ inline int fused_queue(int cls, int gslot) { return cls * N_GSLOTS + (gslot < 0 ? BATCH_GRIDS : gslot); }
 
-template <int STORAGE, int SUM>
-__global__ __launch_bounds__(512) void k_b_weight(BatchDev d, uint32_t chunk, uint32_t tab_cap)
+template <int STORAGE, int SUM, bool PG, int MAXT>
+__global__ __launch_bounds__(MAXT, MAXT >= 512 ? 1 : 3) void k_b_weight(BatchDev d, GridView gp, uint32_t q,
+                                                                         uint32_t chunk, uint32_t tab_cap)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   float4* s_pts = reinterpret_cast<float4*>(smem);
@@ -157,15 +181,14 @@ __global__ __launch_bounds__(512) void k_b_weight(BatchDev d, uint32_t chunk, ui
   float2* s_tab = reinterpret_cast<float2*>(s_part + 2 * 32);
   __shared__ uint32_t s_item;
   __shared__ int s_loaded;
-  constexpr int cls = STORAGE * 2 + SUM;
-  const uint32_t begin = d.counts[4 + 2 * cls], end = d.counts[5 + 2 * cls];
+  const uint32_t begin = d.counts[FQ_BASE + 2 * q], end = d.counts[FQ_BASE + 2 * q + 1];
   if (threadIdx.x == 0)
     s_loaded = -1;
   while (true)
   {
     __syncthreads();
     if (threadIdx.x == 0)
-      s_item = begin + atomicAdd(d.counter + cls, 1u);
+      s_item = begin + atomicAdd(d.counter + q, 1u);
     __syncthreads();
     const uint32_t it = s_item;
     if (it >= end)
@@ -182,7 +205,7 @@ __global__ __launch_bounds__(512) void k_b_weight(BatchDev d, uint32_t chunk, ui
       if (threadIdx.x == 0)
         s_loaded = static_cast<int>(wi.x);
     }
-    b_weigh<STORAGE, SUM>(d, st, wi.y, chunk, s_pts, s_rg, s_part, s_tab);
+    b_weigh<STORAGE, SUM>(d, st, PG ? gp : st.g, wi.y, chunk, s_pts, s_rg, s_part, s_tab);
   }
 }
 
@@ -245,7 +268,7 @@ __global__ __launch_bounds__(SP_WARPS * 32, 3) void k_b_split(BatchDev d, uint32
   __shared__ int s_loaded;
   __shared__ int s_last;
   constexpr int cls = STORAGE * 2 + SUM;
-  const uint32_t begin = d.counts[16 + 2 * cls], end = d.counts[17 + 2 * cls];
+  const uint32_t begin = d.counts[SQ_BASE + 2 * cls], end = d.counts[SQ_BASE + 2 * cls + 1];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (threadIdx.x == 0)
     s_loaded = -1;
@@ -253,7 +276,7 @@ __global__ __launch_bounds__(SP_WARPS * 32, 3) void k_b_split(BatchDev d, uint32
   {
     __syncthreads();
     if (threadIdx.x == 0)
-      s_item = begin + atomicAdd(d.counter + N_CLASSES + cls, 1u);
+      s_item = begin + atomicAdd(d.counter + N_FUSED_Q + cls, 1u);
     __syncthreads();
     const uint32_t it = s_item;
     if (it >= end)
@@ -503,19 +526,24 @@ struct amcl_batch_s
       wt_items, counter, xf, scratch, tile_done;
   PinnedBuf h_cloud, h_ranges, h_steps, h_counts, h_blk, h_wt, h_stats;
   uint32_t n_steps = 0, n_blk = 0, n_wt = 0;
-  uint32_t class_mask = 0;  // weighting classes of the packed step: bits 0-5 fused, 6-11 split
+  uint64_t class_mask = 0;  // weighting queues of the packed step: bit q fused queue q, bit 32 + c split class c
   int split_mode = 0;       // 0 auto, 1 never, 2 always (when the scratch fits)
   uint64_t scratch_cap = 4ull << 30;  // bytes of probability slab a split step may use
   uint64_t n_cloud = 0, n_ranges = 0;
   std::vector<uint32_t> step_slots;  // slot of each step in the last launch
   int threads = 256, chunk = 1024;
   uint32_t tab_cap = 0;
+  // Grids given to the fused weighting launches by value (GridSet): the grid handle of
+  // each entry (null: free) and the views as last packed.
+  const amcl_grid_s* gset_grid[BATCH_GRIDS] = {};
+  GridSet gset{};
   // One instantiated graph per (particle tile, point tile, class mask) in use; all are
   // dropped when a buffer the kernels point at is reallocated or the tables grow.
   struct Graph
   {
     int threads = 0, chunk = 0;
-    uint32_t mask = 0;
+    uint64_t mask = 0;
+    GridSet gset{};  // baked into the captured weighting launches
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaGraphNode_t n_cloud_cp = nullptr, n_ranges_cp = nullptr, n_steps_cp = nullptr, n_counts_cp = nullptr,
@@ -583,39 +611,80 @@ size_t split_smem(const amcl_batch_s* b)
          static_cast<size_t>(SP_RED_STAGES) * SP_RED_PTS * 32 * sizeof(float);
 }
 
-// One persistent launch per weighting class in `mask` (bits 0-5: fused (storage, sum)
-// classes; bits 6-11: the same classes split over points).
-int launch_weight_classes(amcl_batch_s* b, const BatchDev& d, int threads, int chunk, cudaStream_t s, uint32_t mask)
+// Persistent launches of one (storage, sum) class: one per fused queue in `mask`, sized
+// to the blocks that fit on every SM at once.
+template <int STORAGE, int SUM, int MAXT>
+int launch_fused_class(amcl_batch_s* b, const BatchDev& d, int threads, uint32_t chunk, size_t smem, cudaStream_t s,
+                       uint64_t mask)
 {
-  const unsigned grid = static_cast<unsigned>(device_sm_count() * 2);
+  const int cls = weight_class(STORAGE, SUM);
+  for (int slot = 0; slot < N_GSLOTS; ++slot)
+  {
+    const int q = fused_queue(cls, slot < BATCH_GRIDS ? slot : -1);
+    if (!(mask >> q & 1u))
+      continue;
+    int per_sm = 0;
+    if (slot < BATCH_GRIDS)
+    {
+      AMCL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_b_weight<STORAGE, SUM, true, MAXT>,
+                                                                  threads, smem));
+      const unsigned grid = static_cast<unsigned>(device_sm_count() * std::max(per_sm, 1));
+      k_b_weight<STORAGE, SUM, true, MAXT><<<grid, threads, smem, s>>>(d, b->gset.g[slot], static_cast<uint32_t>(q),
+                                                                        chunk, b->tab_cap);
+    }
+    else
+    {
+      AMCL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_b_weight<STORAGE, SUM, false, MAXT>,
+                                                                  threads, smem));
+      const unsigned grid = static_cast<unsigned>(device_sm_count() * std::max(per_sm, 1));
+      k_b_weight<STORAGE, SUM, false, MAXT><<<grid, threads, smem, s>>>(d, GridView{}, static_cast<uint32_t>(q),
+                                                                         chunk, b->tab_cap);
+    }
+    AMCL_LAUNCH_CHECK("k_b_weight");
+  }
+  return AMCL_OK;
+}
+
+template <int MAXT>
+int launch_fused_classes(amcl_batch_s* b, const BatchDev& d, int threads, uint32_t chunk, size_t smem, cudaStream_t s,
+                         uint64_t mask)
+{
+  int rc;
+  if ((rc = launch_fused_class<AMCL_GRID_F32, 0, MAXT>(b, d, threads, chunk, smem, s, mask)) ||
+      (rc = launch_fused_class<AMCL_GRID_F32, 1, MAXT>(b, d, threads, chunk, smem, s, mask)) ||
+      (rc = launch_fused_class<AMCL_GRID_F16, 0, MAXT>(b, d, threads, chunk, smem, s, mask)) ||
+      (rc = launch_fused_class<AMCL_GRID_F16, 1, MAXT>(b, d, threads, chunk, smem, s, mask)) ||
+      (rc = launch_fused_class<AMCL_GRID_U8, 0, MAXT>(b, d, threads, chunk, smem, s, mask)) ||
+      (rc = launch_fused_class<AMCL_GRID_U8, 1, MAXT>(b, d, threads, chunk, smem, s, mask)))
+    return rc;
+  return AMCL_OK;
+}
+
+// The weighting of a packed step: the fused queues in `mask` (bits 0 .. N_FUSED_Q-1),
+// then the split classes (bits SPLIT_MASK_SHIFT + c).
+int launch_weight_classes(amcl_batch_s* b, const BatchDev& d, int threads, int chunk, cudaStream_t s, uint64_t mask)
+{
   const unsigned sgrid = static_cast<unsigned>(device_sm_count() * 3);
   const size_t smem = weight_smem(b, chunk), ssmem = split_smem(b);
   const uint32_t c = static_cast<uint32_t>(chunk);
-  if (mask & (1u << 0))
-    k_b_weight<AMCL_GRID_F32, 0><<<grid, threads, smem, s>>>(d, c, b->tab_cap);
-  if (mask & (1u << 1))
-    k_b_weight<AMCL_GRID_F32, 1><<<grid, threads, smem, s>>>(d, c, b->tab_cap);
-  if (mask & (1u << 2))
-    k_b_weight<AMCL_GRID_F16, 0><<<grid, threads, smem, s>>>(d, c, b->tab_cap);
-  if (mask & (1u << 3))
-    k_b_weight<AMCL_GRID_F16, 1><<<grid, threads, smem, s>>>(d, c, b->tab_cap);
-  if (mask & (1u << 4))
-    k_b_weight<AMCL_GRID_U8, 0><<<grid, threads, smem, s>>>(d, c, b->tab_cap);
-  if (mask & (1u << 5))
-    k_b_weight<AMCL_GRID_U8, 1><<<grid, threads, smem, s>>>(d, c, b->tab_cap);
-  if (mask & (1u << 6))
+  int rc = threads > 256 ? launch_fused_classes<512>(b, d, threads, c, smem, s, mask)
+                         : launch_fused_classes<256>(b, d, threads, c, smem, s, mask);
+  if (rc)
+    return rc;
+  const uint64_t sm = mask >> SPLIT_MASK_SHIFT;
+  if (sm & (1u << 0))
     k_b_split<AMCL_GRID_F32, 0><<<sgrid, SP_WARPS * 32, ssmem, s>>>(d, b->tab_cap);
-  if (mask & (1u << 7))
+  if (sm & (1u << 1))
     k_b_split<AMCL_GRID_F32, 1><<<sgrid, SP_WARPS * 32, ssmem, s>>>(d, b->tab_cap);
-  if (mask & (1u << 8))
+  if (sm & (1u << 2))
     k_b_split<AMCL_GRID_F16, 0><<<sgrid, SP_WARPS * 32, ssmem, s>>>(d, b->tab_cap);
-  if (mask & (1u << 9))
+  if (sm & (1u << 3))
     k_b_split<AMCL_GRID_F16, 1><<<sgrid, SP_WARPS * 32, ssmem, s>>>(d, b->tab_cap);
-  if (mask & (1u << 10))
+  if (sm & (1u << 4))
     k_b_split<AMCL_GRID_U8, 0><<<sgrid, SP_WARPS * 32, ssmem, s>>>(d, b->tab_cap);
-  if (mask & (1u << 11))
+  if (sm & (1u << 5))
     k_b_split<AMCL_GRID_U8, 1><<<sgrid, SP_WARPS * 32, ssmem, s>>>(d, b->tab_cap);
-  AMCL_LAUNCH_CHECK("k_b_weight");
+  AMCL_LAUNCH_CHECK("k_b_split");
   return AMCL_OK;
 }
 
@@ -626,12 +695,24 @@ int smem_attr(K kernel, size_t smem)
   return AMCL_OK;
 }
 
+template <int STORAGE, int SUM>
+int fused_smem_attr(size_t smem)
+{
+  int rc;
+  if ((rc = smem_attr(k_b_weight<STORAGE, SUM, true, 256>, smem)) ||
+      (rc = smem_attr(k_b_weight<STORAGE, SUM, false, 256>, smem)) ||
+      (rc = smem_attr(k_b_weight<STORAGE, SUM, true, 512>, smem)) ||
+      (rc = smem_attr(k_b_weight<STORAGE, SUM, false, 512>, smem)))
+    return rc;
+  return AMCL_OK;
+}
+
 int set_weight_smem(size_t smem, size_t ssmem)
 {
   int rc;
-  if ((rc = smem_attr(k_b_weight<AMCL_GRID_F32, 0>, smem)) || (rc = smem_attr(k_b_weight<AMCL_GRID_F32, 1>, smem)) ||
-      (rc = smem_attr(k_b_weight<AMCL_GRID_F16, 0>, smem)) || (rc = smem_attr(k_b_weight<AMCL_GRID_F16, 1>, smem)) ||
-      (rc = smem_attr(k_b_weight<AMCL_GRID_U8, 0>, smem)) || (rc = smem_attr(k_b_weight<AMCL_GRID_U8, 1>, smem)) ||
+  if ((rc = fused_smem_attr<AMCL_GRID_F32, 0>(smem)) || (rc = fused_smem_attr<AMCL_GRID_F32, 1>(smem)) ||
+      (rc = fused_smem_attr<AMCL_GRID_F16, 0>(smem)) || (rc = fused_smem_attr<AMCL_GRID_F16, 1>(smem)) ||
+      (rc = fused_smem_attr<AMCL_GRID_U8, 0>(smem)) || (rc = fused_smem_attr<AMCL_GRID_U8, 1>(smem)) ||
       (rc = smem_attr(k_b_split<AMCL_GRID_F32, 0>, ssmem)) || (rc = smem_attr(k_b_split<AMCL_GRID_F32, 1>, ssmem)) ||
       (rc = smem_attr(k_b_split<AMCL_GRID_F16, 0>, ssmem)) || (rc = smem_attr(k_b_split<AMCL_GRID_F16, 1>, ssmem)) ||
       (rc = smem_attr(k_b_split<AMCL_GRID_U8, 0>, ssmem)) || (rc = smem_attr(k_b_split<AMCL_GRID_U8, 1>, ssmem)))
@@ -640,7 +721,7 @@ int set_weight_smem(size_t smem, size_t ssmem)
 }
 
 // Enqueues the whole step on the batch stream (also what the graph captures).
-int enqueue_step(amcl_batch_s* b, int threads, int chunk, bool copies, uint32_t mask)
+int enqueue_step(amcl_batch_s* b, int threads, int chunk, bool copies, uint64_t mask)
 {
   cudaStream_t s = b->st.s;
   BatchDev d = batch_dev(b);
@@ -662,13 +743,13 @@ int enqueue_step(amcl_batch_s* b, int threads, int chunk, bool copies, uint32_t 
   }
   k_b_predict<<<grid, NT, 0, s>>>(d);
   AMCL_LAUNCH_CHECK("k_b_predict");
-  if (mask >> N_CLASSES)
+  if (mask >> SPLIT_MASK_SHIFT)
   {
     k_b_xf<<<grid, NT, 0, s>>>(d);
     AMCL_LAUNCH_CHECK("k_b_xf");
   }
   AMCL_CUDA_TRY(cudaMemsetAsync(b->acc.p, 0, static_cast<size_t>(b->max_filters) * ACC_WORDS * 8, s));
-  AMCL_CUDA_TRY(cudaMemsetAsync(b->counter.p, 0, 2 * N_CLASSES * sizeof(unsigned int), s));
+  AMCL_CUDA_TRY(cudaMemsetAsync(b->counter.p, 0, N_COUNTERS * sizeof(unsigned int), s));
   int rc = launch_weight_classes(b, d, threads, chunk, s, mask);
   if (rc)
     return rc;
@@ -688,45 +769,93 @@ int enqueue_step(amcl_batch_s* b, int threads, int chunk, bool copies, uint32_t 
   return AMCL_OK;
 }
 
+// Grid slots of the packed steps: grids already in the batch's GridSet keep their
+// slot; a new grid takes a free slot or one whose grid no step of this pack uses;
+// beyond BATCH_GRIDS distinct grids a step reads its grid from its descriptor.  The
+// set's views are refreshed from the grids, and a changed set drops the captured graphs
+// (the set is a launch argument baked into them).
+void assign_grid_slots(amcl_batch_s* b, SlotStep* hs, const std::vector<const amcl_grid_s*>& step_grid)
+{
+  bool used[BATCH_GRIDS] = {};
+  auto slot_of = [&](const amcl_grid_s* g) {
+    for (int j = 0; j < BATCH_GRIDS; ++j)
+      if (b->gset_grid[j] == g)
+        return j;
+    return -1;
+  };
+  for (const amcl_grid_s* g : step_grid)
+    if (g && slot_of(g) >= 0)
+      used[slot_of(g)] = true;
+  for (const amcl_grid_s* g : step_grid)
+  {
+    if (!g || slot_of(g) >= 0)
+      continue;
+    for (int j = 0; j < BATCH_GRIDS; ++j)
+      if (!used[j])
+      {
+        b->gset_grid[j] = g;
+        used[j] = true;
+        break;
+      }
+  }
+  // Only grids of this pack are read (an entry may name a grid destroyed since).
+  GridSet fresh;
+  std::memcpy(&fresh, &b->gset, sizeof(GridSet));
+  for (const amcl_grid_s* g : step_grid)
+    if (g && slot_of(g) >= 0)
+      std::memcpy(&fresh.g[slot_of(g)], &g->view, sizeof(GridView));
+  if (std::memcmp(&fresh, &b->gset, sizeof(GridSet)) != 0)
+  {
+    b->drop_graphs();
+    std::memcpy(&b->gset, &fresh, sizeof(GridSet));
+  }
+  for (size_t i = 0; i < step_grid.size(); ++i)
+    hs[i].gslot = step_grid[i] ? slot_of(step_grid[i]) : -1;
+}
+
 // Weighting work items of the packed steps.  Fused steps: (step, particle tile of
-// `threads`), grouped by (storage, sum) class, longest scans first within a class
-// (stable, so a filter's tiles stay adjacent and reuse the staged tables).  Split
-// steps: (step, 32-particle tile * slices + 512-point slice), tile-major so a tile's
-// slices run together and its slab is summed while still in L2.  Sets the class mask.
+// `threads`), grouped by fused queue ((storage, sum) class and grid slot), longest
+// scans first within a queue (stable, so a filter's tiles stay adjacent and reuse the
+// staged tables).  Split steps: (step, 32-particle tile * slices + 512-point slice),
+// tile-major so a tile's slices run together and its slab is summed while still in
+// L2.  Sets the class mask.
 void build_weight_items(amcl_batch_s* b, int threads)
 {
   const SlotStep* hs = b->h_steps.as<SlotStep>();
-  auto step_class = [&](uint32_t s) {
+  // Queue of a step: fused queue q (0 .. N_FUSED_Q-1), or N_FUSED_Q + c for split class c.
+  auto step_queue = [&](uint32_t s) {
     const int cls = weight_class(hs[s].g.storage, static_cast<int>(hs[s].cloud_sum));
-    return hs[s].split ? N_CLASSES + cls : cls;
+    return hs[s].split ? N_FUSED_Q + cls : fused_queue(cls, hs[s].gslot);
   };
-  // Steps ordered by class, longest scan first (stable): the items follow step by step.
+  // Steps ordered by queue, longest scan first (stable): the items follow step by step.
   std::vector<uint32_t> order(b->n_steps);
   for (uint32_t s = 0; s < b->n_steps; ++s)
     order[s] = s;
   std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
-    const int cx = step_class(x), cy = step_class(y);
+    const int cx = step_queue(x), cy = step_queue(y);
     return cx != cy ? cx < cy : std::max<uint32_t>(hs[x].N, 1) > std::max<uint32_t>(hs[y].N, 1);
   });
   uint2* hw = b->h_wt.as<uint2>();
   uint32_t* hcnt = b->h_counts.as<uint32_t>();
-  for (int c = 0; c < N_CLASSES; ++c)
-    hcnt[4 + 2 * c] = hcnt[5 + 2 * c] = hcnt[16 + 2 * c] = hcnt[17 + 2 * c] = 0;
-  uint32_t mask = 0, k = 0;
+  for (int w = FQ_BASE; w < COUNT_WORDS; ++w)
+    hcnt[w] = 0;
+  uint64_t mask = 0;
+  uint32_t k = 0;
   int prev = -1;
   for (uint32_t s : order)
   {
-    const int c = step_class(s);
-    const int w = c < N_CLASSES ? 4 + 2 * c : 16 + 2 * (c - N_CLASSES);
-    const uint32_t n = hs[s].split ? ceil_div(hs[s].P, 32) * ceil_div(hs[s].N, SP_PTS) : ceil_div(hs[s].P, threads);
-    if (c != prev)
+    const int qi = step_queue(s);
+    const bool split = qi >= N_FUSED_Q;
+    const int w = split ? SQ_BASE + 2 * (qi - N_FUSED_Q) : FQ_BASE + 2 * qi;
+    const uint32_t n = split ? ceil_div(hs[s].P, 32) * ceil_div(hs[s].N, SP_PTS) : ceil_div(hs[s].P, threads);
+    if (qi != prev)
       hcnt[w] = k;
-    prev = c;
+    prev = qi;
     for (uint32_t j = 0; j < n; ++j)
       hw[k++] = make_uint2(s, j);
     hcnt[w + 1] = k;
     if (n)
-      mask |= 1u << c;
+      mask |= 1ull << (split ? SPLIT_MASK_SHIFT + (qi - N_FUSED_Q) : qi);
   }
   b->n_wt = k;
   b->class_mask = mask;
@@ -806,6 +935,7 @@ int pack_steps(amcl_batch_s* b)
   uint64_t nc = 0, nr = 0;
   b->step_slots.clear();
   const int threads = b->threads;
+  std::vector<const amcl_grid_s*> step_grid;  // grid of each step that gathers
   for (uint32_t si = 0; si < b->slots.size(); ++si)
   {
     BatchSlot& sl = b->slots[si];
@@ -845,12 +975,14 @@ int pack_steps(amcl_batch_s* b)
     st.k1 = static_cast<float>(1.f / (sl.sigma * std::sqrt(2 * M_PI)));
     st.k2 = static_cast<float>(0.5f / (sl.sigma * sl.sigma));
     st.alpha = sl.alpha;
+    st.gslot = -1;
     if (upd)
       st.g = sl.grid->view;
     else
     {
       st.g = GridView{};  // no grid: every particle is outside the map
     }
+    step_grid.push_back(upd && st.N ? sl.grid : nullptr);
     if (sl.predict)
     {
       st.pred.n = sl.P;
@@ -887,6 +1019,7 @@ int pack_steps(amcl_batch_s* b)
     b->step_slots.push_back(si);
     sl.staged = false;
   }
+  assign_grid_slots(b, hs, step_grid);
   b->n_steps = ns;
   b->n_blk = nb;
   b->n_cloud = nc;
@@ -932,7 +1065,7 @@ int graph_update_copies(amcl_batch_s* b, amcl_batch_s::Graph& G)
 }
 
 // Captures and instantiates the step for the current shape and class mask.
-int build_graph(amcl_batch_s* b, uint32_t mask, amcl_batch_s::Graph& G)
+int build_graph(amcl_batch_s* b, uint64_t mask, amcl_batch_s::Graph& G)
 {
   cudaStream_t s = b->st.s;
   AMCL_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
@@ -951,6 +1084,7 @@ int build_graph(amcl_batch_s* b, uint32_t mask, amcl_batch_s::Graph& G)
   G.threads = b->threads;
   G.chunk = b->chunk;
   G.mask = mask;
+  std::memcpy(&G.gset, &b->gset, sizeof(GridSet));
   // Find the memcpy nodes by their destinations.
   size_t nn = 0;
   AMCL_CUDA_TRY(cudaGraphGetNodes(g, nullptr, &nn));
@@ -1076,7 +1210,7 @@ extern "C" int amcl_batch_create(amcl_batch_t* out, uint32_t max_filters, uint64
         (rc = b->cloud.ensure(pts * 16)) || (rc = b->ranges.ensure(rng * 16)) ||
         (rc = b->steps.ensure(static_cast<size_t>(max_filters) * sizeof(SlotStep))) ||
         (rc = b->counts.ensure(COUNT_WORDS * 4)) || (rc = b->blk_items.ensure((cap / NT + max_filters) * sizeof(uint2))) ||
-        (rc = b->wt_items.ensure(items * sizeof(uint2))) || (rc = b->counter.ensure(64)) ||
+        (rc = b->wt_items.ensure(items * sizeof(uint2))) || (rc = b->counter.ensure(N_COUNTERS * sizeof(unsigned int))) ||
         (rc = b->h_cloud.ensure(pts * 16)) || (rc = b->h_ranges.ensure(rng * 16)) ||
         (rc = b->h_steps.ensure(static_cast<size_t>(max_filters) * sizeof(SlotStep))) ||
         (rc = b->h_counts.ensure(COUNT_WORDS * 4)) || (rc = b->h_blk.ensure((cap / NT + max_filters) * sizeof(uint2))) ||
@@ -1382,10 +1516,11 @@ extern "C" int amcl_batch_step(amcl_batch_t b)
     b->tab_cap = tab;
     b->drop_graphs();
   }
-  const uint32_t mask = b->class_mask;
+  const uint64_t mask = b->class_mask;
   amcl_batch_s::Graph* G = nullptr;
   for (auto& g : b->graphs)
-    if (g.threads == b->threads && g.chunk == b->chunk && g.mask == mask)
+    if (g.threads == b->threads && g.chunk == b->chunk && g.mask == mask &&
+        std::memcmp(&g.gset, &b->gset, sizeof(GridSet)) == 0)
       G = &g;
   if (!G)
   {
@@ -1418,7 +1553,7 @@ extern "C" int amcl_batch_step(amcl_batch_t b)
   }
   b->in_flight = true;
   b->steps_done += 1;
-  const int kernels = 6 + (mask >> N_CLASSES ? 1 : 0) + __builtin_popcount(mask);  // the graph's kernels
+  const int kernels = 6 + (mask >> SPLIT_MASK_SHIFT ? 1 : 0) + __builtin_popcountll(mask);  // the graph's kernels
   for (int k = 0; k < kernels; ++k)
     count_launch();
   return AMCL_OK;
@@ -1564,7 +1699,7 @@ extern "C" int amcl_batch_autotune(amcl_batch_t b, int reps, int* best_threads, 
       for (int r = -1; r < reps; ++r)
       {
         AMCL_CUDA_TRY(cudaMemsetAsync(b->acc.p, 0, static_cast<size_t>(b->max_filters) * ACC_WORDS * 8, s));
-        AMCL_CUDA_TRY(cudaMemsetAsync(b->counter.p, 0, 2 * N_CLASSES * sizeof(unsigned int), s));
+        AMCL_CUDA_TRY(cudaMemsetAsync(b->counter.p, 0, N_COUNTERS * sizeof(unsigned int), s));
         cudaEventRecord(e0, s);
         if ((rc = launch_weight_classes(b, d, t, c, s, b->class_mask)))
           return rc;
