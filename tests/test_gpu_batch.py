@@ -154,3 +154,63 @@ def test_stage_many_equals_stage(amcl, world):
         B.close()
     for a, b in zip(*out):
         np.testing.assert_array_equal(a, b)
+
+
+def test_batch_more_grids_than_slots(amcl):
+    """Six filters on six maps in one batch: four grids ride in the launch's grid slots,
+    two are read from their step descriptors.  Then three filters move to two other maps
+    (free slots are reused, the captured graphs rebuilt) and two maps no filter uses are
+    destroyed.  Every filter steps exactly as the same filter stepped alone over the same
+    maps."""
+    import gc
+
+    from amcl3d_gb300.batch import FilterBatch
+
+    maps = [S.make_map(80 + k, size_m=(6.0 + k, 5.0, 3.0), n_boxes=6) for k in range(8)]
+    grids = []
+    for m in maps:
+        G = amcl.Grid3d()
+        assert G.buildGridMap(m.points, m.min, m.max, m.res, S.SENSOR_DEV)
+        grids.append(G)
+    odom = (*MODS, 0.05, 0.01, 0.0, 0.02)
+    moves = {0: 6, 1: 7, 4: 6}  # filter -> map from step 2 on
+    specs = []
+    for k in range(6):
+        pose = S.free_pose(maps[k], 90 + k, height=1.2, clearance=0.4)
+        seq = [k, k, moves.get(k, k), moves.get(k, k)]  # map of each step
+        poses = [pose if g == k else S.free_pose(maps[g], 7 + k, height=1.2, clearance=0.4) for g in seq]
+        scans = [S.ray_cast(maps[g], q, n_max=600, max_range=6.0, seed=99 + k + 10 * s)
+                 for s, (g, q) in enumerate(zip(seq, poses))]
+        specs.append(dict(seq=seq, P=1000 + 700 * k, seed=500 + k, parts=S.particles_around(pose, 1000 + 700 * k, 95 + k),
+                          scans=scans, ranges=S.beacons(maps[k], pose, 3, seed=120 + k)))
+    alone = []
+    for sp in specs:
+        pf = amcl.ParticleFilter(seed=sp["seed"])
+        pf.set_particles(sp["parts"])
+        out = []
+        for s in range(4):
+            pf.predict(*odom)
+            pf.update(grids[sp["seq"][s]], sp["scans"][s], sp["ranges"], 0.5, 0.1, 0.0, 0.0)
+            pf.getMean()
+            pf.resample()
+            out.append(pf.particles())
+        alone.append(out)
+    B = FilterBatch(max_filters=8, max_particles=40000, max_points_per_step=8000)
+    slots = []
+    for sp in specs:
+        sl = B.add(grids[sp["seq"][0]], sp["P"], sp["seed"])
+        B.set_particles(sl, sp["parts"])
+        slots.append(sl)
+    for s in range(4):
+        if s == 2:
+            for i, g in moves.items():
+                B.set_grid(slots[i], grids[g])
+            grids[0] = grids[1] = None  # maps no filter uses any more
+            gc.collect()
+        for sl, sp in zip(slots, specs):
+            B.stage(sl, sp["scans"][s], sp["ranges"], odom, 0.5, 0.1)
+        B.step()
+        B.wait()
+        for i, (sl, sp) in enumerate(zip(slots, specs)):
+            np.testing.assert_array_equal(B.particles(sl, sp["P"]), alone[i][s], err_msg=f"filter {i} step {s}")
+    B.close()
