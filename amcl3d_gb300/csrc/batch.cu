@@ -14,16 +14,18 @@
 // atomic counter (no spin-waits).  Each item is the fused one-thread-per-particle
 // weighting of a single filter, so every filter's weights, sums, mean and resample
 // indices are bit-identical to stepping it alone (the normalisation sums are exact
-// integer sums, independent of how items interleave).
+// integer sums, independent of how items interleave).  Items are queued per (storage,
+// sum) class and grid slot: up to four distinct grids are launch arguments, so their
+// fields come from the constant bank (three 256-thread blocks per SM fit in registers).
 //
 // Small steps (too few particle tiles to fill the GPU, the served case) split the
-// scan instead: items are (32-particle tile, 256-point slice) pairs spread over every
+// scan instead: items are (32-particle tile, 512-point slice) pairs spread over every
 // SM, each writing its probabilities to a [tile][point][lane] scratch slab; the block
 // that completes a tile's last slice (a per-tile atomic counter) sums the tile's slab
 // in cloud order while it is still in L2.  The float sums, and so every result, are
 // the same as the fused path's.  The per-particle transforms of a split step are
-// computed once, after predict.  Each step's graph holds only the weighting kernels
-// of the (storage, sum, fused/split) classes it uses.
+// computed once, after predict.  Each step's graph holds only the weighting launches
+// of the fused queues and split classes it uses.
 //
 // Tuning: the particle tile (threads per block of the weighting kernel) and the point
 // tile (scan points staged in shared memory per iteration) are chosen by
@@ -99,7 +101,7 @@ struct BatchDev
   const float4* cloud;
   const float4* ranges;
   const SlotStep* steps;
-  const uint32_t* counts;  // [0] steps, [1] block items, [2] weight items, [4+2c, 5+2c) class c's item range
+  const uint32_t* counts;  // [0] steps, [1] block items, [2] weight items, then the queues' item ranges
   const uint2* blk_items;  // (step, local block)
   const uint2* wt_items;   // (step, particle tile)
   unsigned int* counter;   // weighting work queues: fused classes, then split classes
@@ -537,8 +539,9 @@ struct amcl_batch_s
   // each entry (null: free) and the views as last packed.
   const amcl_grid_s* gset_grid[BATCH_GRIDS] = {};
   GridSet gset{};
-  // One instantiated graph per (particle tile, point tile, class mask) in use; all are
-  // dropped when a buffer the kernels point at is reallocated or the tables grow.
+  // One instantiated graph per (particle tile, point tile, class mask, grid set) in use;
+  // all are dropped when a buffer the kernels point at is reallocated, the tables grow
+  // or the grid set changes.
   struct Graph
   {
     int threads = 0, chunk = 0;
