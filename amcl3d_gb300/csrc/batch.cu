@@ -127,7 +127,7 @@ __global__ __launch_bounds__(NT) void k_b_predict(BatchDev d)
   }
 }
 
-template <int STORAGE, int SUM>
+template <int STORAGE, int SUM, int TAB>
 __device__ __forceinline__ void b_weigh(const BatchDev& d, const SlotStep& st, const GridView& g, uint32_t tile,
                                         uint32_t chunk, float4* s_pts, const float4* s_rg, X320* s_part,
                                         const float2* s_tab)
@@ -150,7 +150,7 @@ __device__ __forceinline__ void b_weigh(const BatchDev& d, const SlotStep& st, c
   a.acc_wp = d.acc + static_cast<uint64_t>(st.slot) * ACC_WORDS + ACC_WP * NDIG;
   a.acc_wr = d.acc + static_cast<uint64_t>(st.slot) * ACC_WORDS + ACC_WR * NDIG;
   a.yaw_only = st.yaw_only;
-  weigh_block<STORAGE, SUM>(a, g, tile * blockDim.x, chunk, s_pts, s_rg, s_part, s_tab);
+  weigh_block<STORAGE, SUM, TAB>(a, g, tile * blockDim.x, chunk, s_pts, s_rg, s_part, s_tab);
 }
 
 // Persistent: blocks take (filter, particle tile) items of one fused queue until it is
@@ -199,15 +199,17 @@ __global__ __launch_bounds__(MAXT, MAXT >= 512 ? 1 : 3) void k_b_weight(BatchDev
     const SlotStep& st = d.steps[wi.x];
     if (s_loaded != static_cast<int>(wi.x))
     {
-      if (st.N && table_entries(st.g) <= tab_cap)
-        load_tables(st.g, s_tab);
+      if (st.N && tables_staged(st.g))
+        load_tables(st.g, s_tab);  // larger tables stay in global memory
       for (uint32_t i = threadIdx.x; i < st.nr; i += blockDim.x)
         s_rg[i] = d.ranges[st.r_off + i];
       __syncthreads();
       if (threadIdx.x == 0)
         s_loaded = static_cast<int>(wi.x);
     }
-    b_weigh<STORAGE, SUM>(d, st, PG ? gp : st.g, wi.y, chunk, s_pts, s_rg, s_part, s_tab);
+    // slot grids always have staged tables (assign_grid_slots); descriptor grids may not
+    b_weigh<STORAGE, SUM, PG ? TAB_SHARED : TAB_EITHER>(d, st, PG ? gp : st.g, wi.y, chunk, s_pts, s_rg, s_part,
+                                                        s_tab);
   }
 }
 
@@ -290,8 +292,8 @@ __global__ __launch_bounds__(SP_WARPS * 32, 3) void k_b_split(BatchDev d, uint32
     const bool load = s_loaded != static_cast<int>(wi.x);  // read by all before thread 0 updates it below
     if (load)
     {
-      if (table_entries(st.g) <= tab_cap)
-        load_tables(st.g, s_tab);
+      if (tables_staged(st.g))
+        load_tables(st.g, s_tab);  // larger tables stay in global memory
       for (uint32_t i = threadIdx.x; i < st.nr; i += blockDim.x)
         s_rg[i] = d.ranges[st.r_off + i];
     }
@@ -319,11 +321,11 @@ __global__ __launch_bounds__(SP_WARPS * 32, 3) void k_b_split(BatchDev d, uint32
       float* out = const_cast<float*>(slab) + lane;
       const uint32_t k0 = wid * SP_WARP_PTS;
       if (warp_exact && st.yaw_only)
-        tile_values<STORAGE, XF_YAW>(s_pts, k0, SP_WARP_PTS, cnt, s_tab, st.g, rec.xf, out, base);
+        tile_values<STORAGE, XF_YAW, TAB_EITHER>(s_pts, k0, SP_WARP_PTS, cnt, s_tab, st.g, rec.xf, out, base);
       else if (warp_exact)
-        tile_values<STORAGE, XF_EXACT>(s_pts, k0, SP_WARP_PTS, cnt, s_tab, st.g, rec.xf, out, base);
+        tile_values<STORAGE, XF_EXACT, TAB_EITHER>(s_pts, k0, SP_WARP_PTS, cnt, s_tab, st.g, rec.xf, out, base);
       else
-        tile_values<STORAGE, XF_GENERAL>(s_pts, k0, SP_WARP_PTS, cnt, s_tab, st.g, rec.xf, out, base);
+        tile_values<STORAGE, XF_GENERAL, TAB_EITHER>(s_pts, k0, SP_WARP_PTS, cnt, s_tab, st.g, rec.xf, out, base);
     }
     __syncthreads();
     if (threadIdx.x == 0)
@@ -774,7 +776,8 @@ int enqueue_step(amcl_batch_s* b, int threads, int chunk, bool copies, uint64_t 
 
 // Grid slots of the packed steps: grids already in the batch's GridSet keep their
 // slot; a new grid takes a free slot or one whose grid no step of this pack uses;
-// beyond BATCH_GRIDS distinct grids a step reads its grid from its descriptor.  The
+// beyond BATCH_GRIDS distinct grids, and for grids whose locate tables are too large to
+// stage in shared memory, a step reads its grid from its descriptor.  The
 // set's views are refreshed from the grids, and a changed set drops the captured graphs
 // (the set is a launch argument baked into them).
 void assign_grid_slots(amcl_batch_s* b, SlotStep* hs, const std::vector<const amcl_grid_s*>& step_grid)
@@ -791,7 +794,7 @@ void assign_grid_slots(amcl_batch_s* b, SlotStep* hs, const std::vector<const am
       used[slot_of(g)] = true;
   for (const amcl_grid_s* g : step_grid)
   {
-    if (!g || slot_of(g) >= 0)
+    if (!g || slot_of(g) >= 0 || !tables_staged(g->view))  // large tables: descriptor queue
       continue;
     for (int j = 0; j < BATCH_GRIDS; ++j)
       if (!used[j])
@@ -812,8 +815,10 @@ void assign_grid_slots(amcl_batch_s* b, SlotStep* hs, const std::vector<const am
     b->drop_graphs();
     std::memcpy(&b->gset, &fresh, sizeof(GridSet));
   }
+  // a slot's launch reads the tables from shared memory: grids whose tables are not
+  // staged (a grid reloaded at a larger size keeps its entry) use the descriptor queue
   for (size_t i = 0; i < step_grid.size(); ++i)
-    hs[i].gslot = step_grid[i] ? slot_of(step_grid[i]) : -1;
+    hs[i].gslot = step_grid[i] && tables_staged(step_grid[i]->view) ? slot_of(step_grid[i]) : -1;
 }
 
 // Weighting work items of the packed steps.  Fused steps: (step, particle tile of
@@ -1505,11 +1510,12 @@ extern "C" int amcl_batch_step(amcl_batch_t b)
   int rc;
   if ((rc = batch_wait(b)))
     return rc;
-  // table capacity in shared memory: the largest grid among the staged filters
+  // table capacity in shared memory: the largest grid among the staged filters whose
+  // table is staged at all (tables_staged)
   uint32_t tab = 0;
   for (auto& sl : b->slots)
-    if (sl.used && sl.staged && sl.grid && sl.grid->built)
-      tab = std::max<uint32_t>(tab, sl.grid->info.size[0] + sl.grid->info.size[1] + sl.grid->info.size[2] + 3);
+    if (sl.used && sl.staged && sl.grid && sl.grid->built && tables_staged(sl.grid->view))
+      tab = std::max<uint32_t>(tab, table_entries(sl.grid->view));
   if ((rc = pack_steps(b)))
     return rc;
   if (!b->n_steps)

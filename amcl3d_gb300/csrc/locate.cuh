@@ -114,16 +114,50 @@ __device__ __forceinline__ void make_partxf(const GridView& g, float sr, float c
                 : 0;
 }
 
-// Cell index along one axis for an exact X, -1 when the reference rejects the
-// point (X < 0, X >= V, NaN).  floor(X / res) in float is within one cell of the
-// reference's floor(fl64(X / res)); the pair (T[k], T[k+1]) settles it exactly.
-__device__ __forceinline__ int locate_pair(float X, const float2* T2, float V, float inv_res, int size)
+// Locate-table entries staged in shared memory by the weighting kernels (64 KB of
+// float2 pairs).  A grid with more (its three sizes summing above about 8,190 cells)
+// keeps its table in global memory: the table is read only for points near a cell
+// boundary, and staging it would cost occupancy or not fit at all.
+constexpr uint32_t SMEM_TABLE_MAX = 8192;
+
+__host__ __device__ __forceinline__ uint32_t table_entries(const GridView& g)
 {
-  int k = __float2int_rd(fmul(X, inv_res));
-  k = min(max(k, 0), size);
-  const float2 t = T2[k];
+  return g.size[0] + g.size[1] + g.size[2] + 3;
+}
+__host__ __device__ __forceinline__ bool tables_staged(const GridView& g) { return table_entries(g) <= SMEM_TABLE_MAX; }
+
+// Where a kernel reads the locate tables: its shared-memory copy, global memory, or
+// whichever tables_staged(g) says (a branch, taken only near cell boundaries).  The
+// hot kernels fix it at compile time: a run-time choice between the two in the hot
+// loop costs a few percent even though the loads are rare.
+enum : int
+{
+  TAB_SHARED = 0,
+  TAB_GLOBAL = 1,
+  TAB_EITHER = 2
+};
+
+// Pair (T[k], T[k+1]) of axis a (typed loads, so the shared copy keeps its address
+// space).
+template <int TAB>
+__device__ __forceinline__ float2 table_pair(const float2* s_tab, const GridView& g, int a, int k)
+{
+  if (TAB == TAB_SHARED || (TAB == TAB_EITHER && tables_staged(g)))
+    return s_tab[g.toff[a] + k];
+  return __ldg(g.T2 + g.toff[a] + k);
+}
+
+// Cell index along axis a for an exact X, -1 when the reference rejects the point
+// (X < 0, X >= V, NaN).  floor(X / res) in float is within one cell of the
+// reference's floor(fl64(X / res)); the pair (T[k], T[k+1]) settles it exactly.
+template <int TAB>
+__device__ __forceinline__ int locate_pair(float X, const float2* s_tab, const GridView& g, int a)
+{
+  int k = __float2int_rd(fmul(X, g.inv_res[a]));
+  k = min(max(k, 0), static_cast<int>(g.size[a]));
+  const float2 t = table_pair<TAB>(s_tab, g, a, k);
   k = (X < t.x) ? k - 1 : ((X >= t.y) ? k + 1 : k);  // X < 0 ends at -1 (T[0] = 0)
-  return (X < V) ? k : -1;
+  return (X < g.V[a]) ? k : -1;
 }
 
 // Same result as locate_pair for a valid X (0 <= X < V), reading the table only
@@ -146,13 +180,14 @@ __device__ __forceinline__ int floor_bracket(float X, float inv_lo, float inv_hi
 }
 
 // True when a threshold lies within m of X (the estimate may then be on the wrong side).
-__device__ __forceinline__ bool near_threshold(float X, int k, const float2* T2, float V, float m)
+template <int TAB>
+__device__ __forceinline__ bool near_threshold(float X, int k, const float2* s_tab, const GridView& g, int a, float m)
 {
-  if (fabsf(X) <= m || fabsf(V - X) <= m)
+  if (fabsf(X) <= m || fabsf(g.V[a] - X) <= m)
     return true;
   if (k < 0)
     return false;
-  const float2 t = T2[k];
+  const float2 t = table_pair<TAB>(s_tab, g, a, k);
   return (X - t.x <= m) || (t.y - X <= m);
 }
 
@@ -193,6 +228,7 @@ enum : int
 // Grid3d.cpp:178-179 and 185 as 0 <= X < V, one unsigned compare of the bit
 // patterns per axis (X is never -0.0, H being canonicalised; negative X and NaN have
 // patterns above V's), and one branch for the rare point near a cell boundary.
+template <int TAB>
 __device__ __forceinline__ uint32_t settle_cell(const GridView& g, const float2* tab, const float X[3], int k[3],
                                                 bool near)
 {
@@ -204,7 +240,7 @@ __device__ __forceinline__ uint32_t settle_cell(const GridView& g, const float2*
   {
 #pragma unroll
     for (int a = 0; a < 3; ++a)
-      k[a] = locate_pair(X[a], tab + g.toff[a], g.V[a], g.inv_res[a], static_cast<int>(g.size[a]));
+      k[a] = locate_pair<TAB>(X[a], tab, g, a);
     valid = (k[0] | k[1] | k[2]) >= 0;
   }
   if (!valid)
@@ -215,7 +251,7 @@ __device__ __forceinline__ uint32_t settle_cell(const GridView& g, const float2*
 // Grid cell of scan point (px, py, pz0) for the particle, 0xFFFFFFFF when the
 // reference skips it.  pz0 is s.z + 0.0f (Grid3d.cpp:174-176).  `tab` is the pair
 // table (in shared memory in the kernels).
-template <int MODE>
+template <int MODE, int TAB>
 __device__ __forceinline__ uint32_t cell_of_point(const GridView& g, const float2* tab, const PartXf& p, float px,
                                                   float py, float pz0)
 {
@@ -244,7 +280,7 @@ __device__ __forceinline__ uint32_t cell_of_point(const GridView& g, const float
       X[a] = fadd(s[a], p.H[a]);
       k[a] = floor_bracket(X[a], g.inv_lo[a], g.inv_hi[a], near);
     }
-    return settle_cell(g, tab, X, k, near);
+    return settle_cell<TAB>(g, tab, X, k, near);
   }
   bool amb = false;
 #pragma unroll
@@ -252,9 +288,8 @@ __device__ __forceinline__ uint32_t cell_of_point(const GridView& g, const float
   {
     float m;
     const float X = xform_axis(s[a], p.H[a], p.L[a], m);
-    const float2* T = tab + g.toff[a];
-    k[a] = locate_pair(X, T, g.V[a], g.inv_res[a], static_cast<int>(g.size[a]));
-    amb |= near_threshold(X, k[a], T, g.V[a], m);
+    k[a] = locate_pair<TAB>(X, tab, g, a);
+    amb |= near_threshold<TAB>(X, k[a], tab, g, a, m);
   }
   if (amb)
   {
@@ -263,7 +298,7 @@ __device__ __forceinline__ uint32_t cell_of_point(const GridView& g, const float
     for (int a = 0; a < 3; ++a)
     {
       const float X = __double2float_rn(__dadd_rn(static_cast<double>(s[a]), p.off[a]));
-      k[a] = locate_pair(X, tab + g.toff[a], g.V[a], g.inv_res[a], static_cast<int>(g.size[a]));
+      k[a] = locate_pair<TAB>(X, tab, g, a);
     }
   }
   return cell_index(g, k[0], k[1], k[2]);
@@ -315,6 +350,7 @@ __device__ __forceinline__ PartYaw2 pair_yaw(const GridView& g, const PartXf& p)
   return q;
 }
 
+template <int TAB>
 __device__ __forceinline__ uint32_t cell_of_point_yaw2(const GridView& g, const float2* tab, const PartYaw2& q,
                                                        float4 xxyy, float pz0)
 {
@@ -329,7 +365,7 @@ __device__ __forceinline__ uint32_t cell_of_point_yaw2(const GridView& g, const 
   const float X[3] = { X01.x, X01.y, Xz };
   int k[3] = { __float_as_int(lo.x) - 0x4B400000, __float_as_int(lo.y) - 0x4B400000,
                __float_as_int(loz) - 0x4B400000 };
-  return settle_cell(g, tab, X, k, near);
+  return settle_cell<TAB>(g, tab, X, k, near);
 }
 
 template <int STORAGE>

@@ -32,7 +32,7 @@ namespace
 constexpr int WT_THREADS = 192;  // 6 warps; 4 blocks per SM by registers (80 per thread)
 constexpr int WT_CHUNK = 1024;  // points staged per block iteration (16 KB)
 
-template <int STORAGE, int SUM>
+template <int STORAGE, int SUM, int TAB>
 __global__ __launch_bounds__(WT_THREADS, 4) void k_weight_fused(WeightArgs a, GridView g)
 {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -41,11 +41,11 @@ __global__ __launch_bounds__(WT_THREADS, 4) void k_weight_fused(WeightArgs a, Gr
   X320* s_part = reinterpret_cast<X320*>(s_rg + MAX_RANGES);
   float2* s_tab = reinterpret_cast<float2*>(s_part + 2 * (WT_THREADS / 32));
   // The locate tables are only read per point (a range-only update has no grid).
-  if (a.N)
+  if (a.N && TAB == TAB_SHARED)
     load_tables(g, s_tab);
   for (uint32_t i = threadIdx.x; i < a.nr; i += blockDim.x)
     s_rg[i] = a.ranges[i];
-  weigh_block<STORAGE, SUM>(a, g, blockIdx.x * blockDim.x, WT_CHUNK, s_pts, s_rg, s_part, s_tab);
+  weigh_block<STORAGE, SUM, TAB>(a, g, blockIdx.x * blockDim.x, WT_CHUNK, s_pts, s_rg, s_part, s_tab);
 }
 
 // ---- two-phase ----------------------------------------------------------------------------
@@ -65,10 +65,9 @@ __global__ __launch_bounds__(TP_WARPS * 32) void k_weight_tile_vals(WeightArgs a
   extern __shared__ __align__(16) unsigned char smem[];
   float4* s_pts = reinterpret_cast<float4*>(smem);
   PartRec* s_rec = reinterpret_cast<PartRec*>(s_pts + TP_PTS_PER_BLOCK);
-  float2* s_tab = reinterpret_cast<float2*>(s_rec + 32);
-  const uint32_t ntab = table_entries(g);
-  for (uint32_t i = threadIdx.x; i < ntab; i += blockDim.x)
-    s_tab[i] = g.T2[i];
+  float2* tab = reinterpret_cast<float2*>(s_rec + 32);  // used only when the grid's tables are staged
+  if (tables_staged(g))
+    load_tables(g, tab);
   const uint32_t tile = blockIdx.x;
   const uint32_t base = blockIdx.y * TP_PTS_PER_BLOCK;
   const uint32_t cnt = base < a.N ? min(static_cast<uint32_t>(TP_PTS_PER_BLOCK), a.N - base) : 0u;
@@ -101,11 +100,11 @@ __global__ __launch_bounds__(TP_WARPS * 32) void k_weight_tile_vals(WeightArgs a
   float* out = a.scratch + (static_cast<uint64_t>(tile) * a.N) * 32 + lane;
   const uint32_t k0 = wid * TP_PTS_PER_WARP;
   if (warp_exact && a.yaw_only)
-    tile_values<STORAGE, XF_YAW>(s_pts, k0, TP_PTS_PER_WARP, cnt, s_tab, g, rec.xf, out, base);
+    tile_values<STORAGE, XF_YAW, TAB_EITHER>(s_pts, k0, TP_PTS_PER_WARP, cnt, tab, g, rec.xf, out, base);
   else if (warp_exact)
-    tile_values<STORAGE, XF_EXACT>(s_pts, k0, TP_PTS_PER_WARP, cnt, s_tab, g, rec.xf, out, base);
+    tile_values<STORAGE, XF_EXACT, TAB_EITHER>(s_pts, k0, TP_PTS_PER_WARP, cnt, tab, g, rec.xf, out, base);
   else
-    tile_values<STORAGE, XF_GENERAL>(s_pts, k0, TP_PTS_PER_WARP, cnt, s_tab, g, rec.xf, out, base);
+    tile_values<STORAGE, XF_GENERAL, TAB_EITHER>(s_pts, k0, TP_PTS_PER_WARP, cnt, tab, g, rec.xf, out, base);
 }
 
 constexpr int TR_STAGE_PTS = 128;  // points per stage: 128 x 32 lanes x 4 B = 16 KB
@@ -217,14 +216,20 @@ template <int STORAGE, int SUM>
 int launch_fused(const WeightArgs& a, const GridView& g, cudaStream_t s)
 {
   const size_t smem = WT_CHUNK * sizeof(float4) + MAX_RANGES * sizeof(float4) + 2 * (WT_THREADS / 32) * sizeof(X320) +
-                      (a.N ? table_bytes(g) : 0);
+                      (a.N && tables_staged(g) ? table_bytes(g) : 0);
   static bool attr_done = false;
   if (!attr_done)
   {
-    cudaFuncSetAttribute(k_weight_fused<STORAGE, SUM>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_weight_fused<STORAGE, SUM, TAB_SHARED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         200 * 1024);
+    cudaFuncSetAttribute(k_weight_fused<STORAGE, SUM, TAB_GLOBAL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         200 * 1024);
     attr_done = true;
   }
-  k_weight_fused<STORAGE, SUM><<<ceil_div(a.P, WT_THREADS), WT_THREADS, smem, s>>>(a, g);
+  if (tables_staged(g))
+    k_weight_fused<STORAGE, SUM, TAB_SHARED><<<ceil_div(a.P, WT_THREADS), WT_THREADS, smem, s>>>(a, g);
+  else
+    k_weight_fused<STORAGE, SUM, TAB_GLOBAL><<<ceil_div(a.P, WT_THREADS), WT_THREADS, smem, s>>>(a, g);
   AMCL_LAUNCH_CHECK("k_weight_fused");
   return AMCL_OK;
 }
@@ -232,7 +237,7 @@ int launch_fused(const WeightArgs& a, const GridView& g, cudaStream_t s)
 template <int STORAGE, int SUM>
 int launch_two_phase(const WeightArgs& a, const GridView& g, cudaStream_t s)
 {
-  const size_t smem1 = TP_PTS_PER_BLOCK * sizeof(float4) + 32 * sizeof(PartRec) + table_bytes(g);
+  const size_t smem1 = TP_PTS_PER_BLOCK * sizeof(float4) + 32 * sizeof(PartRec) + (tables_staged(g) ? table_bytes(g) : 0);
   const size_t smem2 = static_cast<size_t>(TR_STAGES) * TR_STAGE_PTS * 32 * sizeof(float);
   static bool attr_done = false;
   if (!attr_done)

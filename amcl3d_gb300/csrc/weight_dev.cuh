@@ -63,7 +63,7 @@ struct CloudSum
 // Adds the points [0, cnt) of a staged chunk (cnt a multiple of UNROLL, padding
 // points NaN) in order.  Points are float4 (x, y, z + 0, -), or with YL the
 // yaw-only staging: (x, x, y, y) in s_pts and z + 0 in s_z.
-template <int STORAGE, int SUM, int MODE, bool YL>
+template <int STORAGE, int SUM, int MODE, bool YL, int TAB>
 __device__ __forceinline__ void weigh_chunk(const float4* s_pts, const float* s_z, uint32_t cnt, const float2* s_tab,
                                             const GridView& g, const PartXf& xf, CloudSum<SUM>& acc)
 {
@@ -74,8 +74,8 @@ __device__ __forceinline__ void weigh_chunk(const float4* s_pts, const float* s_
     for (int j = 0; j < UNROLL; ++j)
     {
       const float4 s = s_pts[k + j];
-      cell[j] = YL ? cell_of_point<MODE>(g, s_tab, xf, s.x, s.z, s_z[k + j])
-                   : cell_of_point<MODE>(g, s_tab, xf, s.x, s.y, s.z);
+      cell[j] = YL ? cell_of_point<MODE, TAB>(g, s_tab, xf, s.x, s.z, s_z[k + j])
+                   : cell_of_point<MODE, TAB>(g, s_tab, xf, s.x, s.y, s.z);
     }
     float v[UNROLL];
 #pragma unroll
@@ -90,7 +90,7 @@ __device__ __forceinline__ void weigh_chunk(const float4* s_pts, const float* s_
 
 // weigh_chunk of the yaw-only mode on the yaw-only staging, x and y paired, YAW_UNROLL
 // points per group (cnt a multiple of it).
-template <int STORAGE, int SUM>
+template <int STORAGE, int SUM, int TAB>
 __device__ __forceinline__ void weigh_chunk_yaw2(const float4* s_pts, const float* s_z, uint32_t cnt,
                                                  const float2* s_tab, const GridView& g, const PartYaw2& q,
                                                  CloudSum<SUM>& acc)
@@ -111,7 +111,7 @@ __device__ __forceinline__ void weigh_chunk_yaw2(const float4* s_pts, const floa
     uint32_t cell[YAW_UNROLL];
 #pragma unroll
     for (int j = 0; j < YAW_UNROLL; ++j)
-      cell[j] = cell_of_point_yaw2(g, s_tab, q, s_pts[k + j], zs[j]);
+      cell[j] = cell_of_point_yaw2<TAB>(g, s_tab, q, s_pts[k + j], zs[j]);
     float v[YAW_UNROLL];
 #pragma unroll
     for (int j = 0; j < YAW_UNROLL; ++j)
@@ -127,7 +127,7 @@ __device__ __forceinline__ void weigh_chunk_yaw2(const float4* s_pts, const floa
 // points from k0): each lane writes its particle's cell probability, or -1 for a
 // point the reference skips, to out[(base + k) * 32] for k < cnt, the
 // [tile][point][lane] slab that an in-order pass sums afterwards.
-template <int STORAGE, int MODE>
+template <int STORAGE, int MODE, int TAB>
 __device__ __forceinline__ void tile_values(const float4* s_pts, uint32_t k0, uint32_t npts, uint32_t cnt,
                                             const float2* s_tab, const GridView& g, const PartXf& xf, float* out,
                                             uint32_t base)
@@ -139,7 +139,7 @@ __device__ __forceinline__ void tile_values(const float4* s_pts, uint32_t k0, ui
     for (int j = 0; j < UNROLL; ++j)
     {
       const float4 s = s_pts[k0 + kk + j];
-      cell[j] = cell_of_point<MODE>(g, s_tab, xf, s.x, s.y, s.z);
+      cell[j] = cell_of_point<MODE, TAB>(g, s_tab, xf, s.x, s.y, s.z);
     }
 #pragma unroll
     for (int j = 0; j < UNROLL; ++j)
@@ -211,7 +211,6 @@ __device__ __forceinline__ void block_exact_pair(float va, float vb, bool take, 
   }
 }
 
-__device__ __forceinline__ uint32_t table_entries(const GridView& g) { return g.size[0] + g.size[1] + g.size[2] + 3; }
 
 // Copies the grid's locate pairs into shared memory (all threads of the block).
 __device__ __forceinline__ void load_tables(const GridView& g, float2* s_tab)
@@ -226,7 +225,7 @@ __device__ __forceinline__ void load_tables(const GridView& g, float2* s_tab)
 // s_tab (when a.N > 0) and s_rg.  s_pts holds `chunk` float4 (a multiple of UNROLL):
 // as many points per stage, or 4/5 as many (a multiple of YAW_UNROLL) in the yaw-only
 // staging.  Every thread of the block must call this.
-template <int STORAGE, int SUM>
+template <int STORAGE, int SUM, int TAB>
 __device__ __forceinline__ void weigh_block(const WeightArgs& a, const GridView& g, uint32_t p0, uint32_t chunk,
                                             float4* s_pts, const float4* s_rg, X320* s_part, const float2* s_tab)
 {
@@ -278,13 +277,13 @@ __device__ __forceinline__ void weigh_block(const WeightArgs& a, const GridView&
     if (!inm)
       continue;
     if (mode == XF_YAW)
-      weigh_chunk_yaw2<STORAGE, SUM>(s_pts, s_z, cnt8, s_tab, g, q, acc);
+      weigh_chunk_yaw2<STORAGE, SUM, TAB>(s_pts, s_z, cnt8, s_tab, g, q, acc);
     else if (mode == XF_EXACT)
-      weigh_chunk<STORAGE, SUM, XF_EXACT, false>(s_pts, s_z, cnt8, s_tab, g, xf, acc);
+      weigh_chunk<STORAGE, SUM, XF_EXACT, false, TAB>(s_pts, s_z, cnt8, s_tab, g, xf, acc);
     else if (yl)
-      weigh_chunk<STORAGE, SUM, XF_GENERAL, true>(s_pts, s_z, cnt8, s_tab, g, xf, acc);
+      weigh_chunk<STORAGE, SUM, XF_GENERAL, true, TAB>(s_pts, s_z, cnt8, s_tab, g, xf, acc);
     else
-      weigh_chunk<STORAGE, SUM, XF_GENERAL, false>(s_pts, s_z, cnt8, s_tab, g, xf, acc);
+      weigh_chunk<STORAGE, SUM, XF_GENERAL, false, TAB>(s_pts, s_z, cnt8, s_tab, g, xf, acc);
   }
   float wpv = 0.0f, wrv = 0.0f;
   if (inm)

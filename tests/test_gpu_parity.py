@@ -194,6 +194,36 @@ def test_cloud_weights_one_thread_per_particle(amcl, roll, pitch):
     np.testing.assert_array_equal(w_gpu, O.cloud_weights(g, poses, scan, roll, pitch, yaw_trig=1))
 
 
+@pytest.mark.parametrize("nx", [2**21 - 1, 2**21 + 3])
+def test_cloud_weights_long_axis(amcl, nx):
+    """An x axis of about 2^21 cells (x up to 105 km at 0.05 m): below 2^21 cells the
+    two bracket floors settle the cell, from 2^21 on every point goes through the
+    threshold table (the upper bracket is +inf).  Particles spread along the whole
+    axis, against the oracle on the same cells."""
+    size = (nx, 2, 2)
+    res = 0.05
+    rng = np.random.default_rng(11)
+    prob = rng.random(nx * 4, dtype=np.float32)
+    dist = np.zeros_like(prob)
+    mx = tuple(float(s * res) for s in size)
+    G = amcl.Grid3d()
+    G.load_cells({"min": (0.0, 0.0, 0.0), "max": mx, "size": size, "resolution": res, "sensor_dev": 0.05}, dist,
+                 prob)
+    P, N = 4096, 512
+    poses = np.zeros((P, 4), np.float32)
+    poses[:, 0] = rng.uniform(0.0, mx[0], P).astype(np.float32)
+    poses[:, 0][:8] = np.float32(mx[0]) - np.arange(8, dtype=np.float32)  # next to the far end
+    scan = np.zeros((N, 3), np.float32)
+    scan[:, 0] = rng.uniform(-20.0, 20.0, N).astype(np.float32)
+    scan[:, 1] = rng.uniform(0.0, 0.1, N).astype(np.float32)
+    scan[:, 2] = rng.uniform(0.0, 0.1, N).astype(np.float32)
+    w_gpu = G.computeCloudWeights(poses, scan)
+    g = O.GridData((0.0, 0.0, 0.0), mx, res, size, prob)
+    w_orc = O.cloud_weights(g, poses, scan, 0.0, 0.0, yaw_trig=1)
+    np.testing.assert_array_equal(w_gpu, w_orc)
+    assert (w_orc > 0).mean() > 0.9
+
+
 # ---- update / normalise / mean --------------------------------------------------------------------
 
 def run_update(amcl, G, parts, scan, ranges, alpha=0.5, sigma=0.1, roll=0.0, pitch=0.0, kernel=0, cloud_sum=0):
