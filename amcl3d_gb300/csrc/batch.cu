@@ -174,7 +174,7 @@ __host__ __device__ inline int fused_queue(int cls, int gslot) { return cls * N_
 
 template <int STORAGE, int SUM, bool PG, int MAXT>
 __global__ __launch_bounds__(MAXT, MAXT >= 512 ? 1 : 3) void k_b_weight(BatchDev d, GridView gp, uint32_t q,
-                                                                         uint32_t chunk, uint32_t tab_cap)
+                                                                         uint32_t chunk)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   float4* s_pts = reinterpret_cast<float4*>(smem);
@@ -635,7 +635,7 @@ int launch_fused_class(amcl_batch_s* b, const BatchDev& d, int threads, uint32_t
                                                                   threads, smem));
       const unsigned grid = static_cast<unsigned>(device_sm_count() * std::max(per_sm, 1));
       k_b_weight<STORAGE, SUM, true, MAXT><<<grid, threads, smem, s>>>(d, b->gset.g[slot], static_cast<uint32_t>(q),
-                                                                        chunk, b->tab_cap);
+                                                                        chunk);
     }
     else
     {
@@ -643,7 +643,7 @@ int launch_fused_class(amcl_batch_s* b, const BatchDev& d, int threads, uint32_t
                                                                   threads, smem));
       const unsigned grid = static_cast<unsigned>(device_sm_count() * std::max(per_sm, 1));
       k_b_weight<STORAGE, SUM, false, MAXT><<<grid, threads, smem, s>>>(d, GridView{}, static_cast<uint32_t>(q),
-                                                                         chunk, b->tab_cap);
+                                                                         chunk);
     }
     AMCL_LAUNCH_CHECK("k_b_weight");
   }
