@@ -397,7 +397,9 @@ def run_ours(args, cfg, rank, world, local_rank):
                      "peak_source": peak_kind, "kernel": "cloud weight (per-particle scan gather)",
                      "kernel_ms_per_launch": (cw_ms / cw_n) if cw_n else None,
                      "traffic_unit": "DRAM bytes per launch (ncu, full-size capture)",
-                     "limiter": "instruction issue: the cell gathers are L2-resident (ncu: >99% L2 hits)",
+                     "limiter": "instruction issue and dependent-instruction latency (37 warp instructions per "
+                                "particle x point, 69% issue-active); the cell gathers are L2-resident "
+                                "(ncu: >99% L2 hits)",
                      "algorithmic_bytes_per_launch": alg_bytes},
         "kernel_ms": {k: (v[0] / v[1] if v[1] else None) for k, v in prof.items()},
     }
