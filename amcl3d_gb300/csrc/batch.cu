@@ -252,7 +252,7 @@ __device__ __forceinline__ unsigned int atomic_add_acq_rel_gpu(unsigned int* p, 
 // Offset (floats) of the reduction buffers in a split block's shared memory.
 __host__ __device__ inline uint32_t split_red_offset(uint32_t tab_cap)
 {
-  const uint32_t bytes = SP_PTS * 16 + MAX_RANGES * 16 + tab_cap * 8;
+  const uint32_t bytes = SP_PTS * 16 + MAX_RANGES * 16 + (tab_cap + 3) * 4;  // staged tables: floats
   return ((bytes + 15) & ~15u) / 4;
 }
 
@@ -607,7 +607,7 @@ BatchDev batch_dev(amcl_batch_s* b)
 size_t weight_smem(const amcl_batch_s* b, int chunk)
 {
   return static_cast<size_t>(chunk) * sizeof(float4) + MAX_RANGES * sizeof(float4) + 64 * sizeof(X320) +
-         static_cast<size_t>(b->tab_cap) * sizeof(float2);
+         (static_cast<size_t>(b->tab_cap) + 3) * sizeof(float);  // staged tables: floats (load_tables)
 }
 
 size_t split_smem(const amcl_batch_s* b)

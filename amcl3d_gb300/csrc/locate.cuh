@@ -114,8 +114,8 @@ __device__ __forceinline__ void make_partxf(const GridView& g, float sr, float c
                 : 0;
 }
 
-// Locate-table entries staged in shared memory by the weighting kernels (64 KB of
-// float2 pairs).  A grid with more (its three sizes summing above about 8,190 cells)
+// Locate-table entries staged in shared memory by the weighting kernels (32 KB as
+// single floats, load_tables).  A grid with more (its three sizes summing above about 8,190 cells)
 // keeps its table in global memory: the table is read only for points near a cell
 // boundary, and staging it would cost occupancy or not fit at all.
 constexpr uint32_t SMEM_TABLE_MAX = 8192;
@@ -125,6 +125,8 @@ __host__ __device__ __forceinline__ uint32_t table_entries(const GridView& g)
   return g.size[0] + g.size[1] + g.size[2] + 3;
 }
 __host__ __device__ __forceinline__ bool tables_staged(const GridView& g) { return table_entries(g) <= SMEM_TABLE_MAX; }
+// Floats of the shared-memory copy (load_tables): size + 2 thresholds per axis.
+__host__ __device__ __forceinline__ uint32_t table_staged_floats(const GridView& g) { return table_entries(g) + 3; }
 
 // Where a kernel reads the locate tables: its shared-memory copy, global memory, or
 // whichever tables_staged(g) says (a branch, taken only near cell boundaries).  The
@@ -138,12 +140,16 @@ enum : int
 };
 
 // Pair (T[k], T[k+1]) of axis a (typed loads, so the shared copy keeps its address
-// space).
+// space): two adjacent floats of the staged copy, or one pair from global memory.
 template <int TAB>
 __device__ __forceinline__ float2 table_pair(const float2* s_tab, const GridView& g, int a, int k)
 {
   if (TAB == TAB_SHARED || (TAB == TAB_EITHER && tables_staged(g)))
-    return s_tab[g.toff[a] + k];
+  {
+    const float* sT = reinterpret_cast<const float*>(s_tab);
+    const int j = static_cast<int>(g.toff[a]) + a + k;
+    return make_float2(sT[j], sT[j + 1]);
+  }
   return __ldg(g.T2 + g.toff[a] + k);
 }
 

@@ -209,7 +209,7 @@ __global__ __launch_bounds__(32) void k_weight_tile_reduce(WeightArgs a, GridVie
 
 size_t table_bytes(const GridView& g)
 {
-  return (static_cast<size_t>(g.size[0]) + g.size[1] + g.size[2] + 3) * sizeof(float2);
+  return static_cast<size_t>(table_staged_floats(g)) * sizeof(float);
 }
 
 template <int STORAGE, int SUM>

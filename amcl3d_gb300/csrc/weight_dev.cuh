@@ -212,12 +212,22 @@ __device__ __forceinline__ void block_exact_pair(float va, float vb, bool take, 
 }
 
 
-// Copies the grid's locate pairs into shared memory (all threads of the block).
+// Copies the grid's locate thresholds into shared memory (all threads of the block),
+// as single floats: axis a's T[0..size+1] at float offset toff[a] + a (T[size+1] = +inf
+// from the last pair's upper half), table_staged_floats(g) floats in all.  Half the
+// bytes of the pairs leaves the SM's L1 more room for the cell gathers.
 __device__ __forceinline__ void load_tables(const GridView& g, float2* s_tab)
 {
+  float* sT = reinterpret_cast<float*>(s_tab);
   const uint32_t ntab = table_entries(g);
   for (uint32_t i = threadIdx.x; i < ntab; i += blockDim.x)
-    s_tab[i] = g.T2[i];
+  {
+    const int a = i >= g.toff[2] ? 2 : (i >= g.toff[1] ? 1 : 0);
+    const float2 t = g.T2[i];
+    sT[i + a] = t.x;
+    if (i == g.toff[a] + g.size[a])
+      sT[i + a + 1] = t.y;
+  }
 }
 
 // One block of particles [p0, p0 + blockDim) of one filter, one thread per particle
