@@ -25,7 +25,8 @@ CPP = PKG / "cpp"
 BUILD = PKG / "_build"
 LIB = PKG / "_lib"
 INCLUDE = ROOT / "include"
-SHIM = ROOT / "oracle" / "shim"
+# Stand-in ROS/PCL/octomap/boost headers (types only) for builds without ROS installed.
+SHIM = ROOT / "tests" / "stand_in"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
@@ -107,7 +108,9 @@ def build_oracle() -> None:
     reference filter core compiled verbatim (test infrastructure only)."""
     mk = ROOT / "oracle" / "Makefile"
     _run(["make", "-s", "-C", str(mk.parent), "all"])
-    ref = Path(os.environ.get("AMCL3D_REF_SRC", "/root/reference/amcl3d/src"))
+    # the reference checkout: AMCL3D_REF_ROOT, else a `reference` directory beside this one
+    ref_root = Path(os.environ.get("AMCL3D_REF_ROOT", str(ROOT.parent / "reference")))
+    ref = Path(os.environ.get("AMCL3D_REF_SRC", str(ref_root / "amcl3d" / "src")))
     if (ref / "ParticleFilter.cpp").exists():
         _run(["make", "-s", "-C", str(mk.parent), "ref", f"REF_SRC={ref}"])
 

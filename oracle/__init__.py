@@ -11,7 +11,7 @@ Two oracles:
   semantics of the GPU build restated here with ``math.fsum`` / Python integers;
 * ``_ref/libamcl3d_ref.so`` (``ref_harness.cpp``): the reference's own
   ParticleFilter.cpp / Grid3d.cpp / PointCloudTools.cpp compiled verbatim against
-  the stand-in headers in ``shim/``.  It exists only where the reference tree is
+  the stand-in headers in ``tests/stand_in/``.  It exists only where the reference tree is
   available at build time; the committed golden fixtures under ``tests/golden``
   carry its outputs elsewhere.
 """

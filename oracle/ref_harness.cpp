@@ -1,6 +1,6 @@
 // Test infrastructure: extern "C" driver around the UNMODIFIED amcl3d filter core
 // (ParticleFilter.cpp, Grid3d.cpp, PointCloudTools.cpp compiled from the reference
-// tree against the stand-in headers in shim/).  Only the test suite, the smoke
+// tree against the stand-in headers in tests/stand_in/).  Only the test suite, the smoke
 // check and the CPU-baseline leg of the benchmark load the resulting library.
 //
 // Private members are reached by the test-only `#define private public` below:

@@ -1,7 +1,7 @@
 """Generates the committed golden fixtures under tests/golden/.
 
-Run in a checkout where the reference tree is readable (default
-/root/reference, override with AMCL3D_REF_ROOT) after `make -C oracle all ref`:
+Run where the reference tree is readable (a `reference` checkout beside this
+repository by default, override with AMCL3D_REF_ROOT) after `make -C oracle all ref`:
 
     python tests/golden/make_golden.py
 
@@ -36,7 +36,8 @@ sys.path.insert(0, str(ROOT))
 import oracle as O  # noqa: E402
 from amcl3d_gb300 import synth as S  # noqa: E402
 
-REF_ROOT = Path(os.environ.get("AMCL3D_REF_ROOT", "/root/reference"))
+# the reference checkout: AMCL3D_REF_ROOT, else a `reference` directory beside this repository
+REF_ROOT = Path(os.environ.get("AMCL3D_REF_ROOT", str(ROOT.parent / "reference")))
 DATA = REF_ROOT / "amcl3d" / "tests" / "data"
 
 
