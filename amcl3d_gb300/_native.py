@@ -27,7 +27,7 @@ STATUS = {
     8: "AMCL_ENOTSUP",
 }
 GRID_F32, GRID_F16, GRID_U8 = 0, 1, 2
-OPT_CLOUD_SUM, OPT_RESAMPLE_PREFIX, OPT_WEIGHT_KERNEL, OPT_SEED = 1, 2, 3, 4
+OPT_CLOUD_SUM, OPT_RESAMPLE_PREFIX, OPT_WEIGHT_KERNEL, OPT_SEED, OPT_WAIT_PROBE = 1, 2, 3, 4, 5
 PROF_NAMES = ("cloud_weight", "normalize", "resample", "predict", "distance_field")
 
 

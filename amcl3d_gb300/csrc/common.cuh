@@ -225,6 +225,22 @@ struct ProfScope
 
 inline unsigned ceil_div(uint64_t a, uint64_t b) { return static_cast<unsigned>((a + b - 1) / b); }
 
+// Runs `set` (returning an AMCL status) once for the current device and remembers
+// success per device ordinal (0-63) in `done`: kernel attributes are per device.
+template <typename F>
+int once_per_device(std::atomic<uint64_t>& done, F set)
+{
+  int dev = 0;
+  AMCL_CUDA_TRY(cudaGetDevice(&dev));
+  const uint64_t bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0ull;
+  if (bit && (done.load(std::memory_order_acquire) & bit))
+    return AMCL_OK;
+  const int rc = set();
+  if (rc == AMCL_OK && bit)
+    done.fetch_or(bit, std::memory_order_acq_rel);
+  return rc;
+}
+
 int device_sm_count();
 
 }  // namespace amcl

@@ -185,7 +185,7 @@ struct amcl_pf_s
   bool blocksum_valid = false;
   bool record = false;
   bool have_ridx = false;
-  int opt_cloud_sum = 0, opt_prefix = 0, opt_kernel = 0;
+  int opt_cloud_sum = 0, opt_prefix = 0, opt_kernel = 0, opt_wait_probe = 0;
   Profiler prof;
   std::mutex mu;
 };
@@ -318,6 +318,8 @@ int pf_update_impl(amcl_pf_s* pf, amcl_grid_s* g, const float4* cloud_dev, uint3
       return rc;
     a.scratch = pf->scratch.as<float>();
     a.scratch_floats = pf->scratch.bytes / 4;
+    a.wait_probe = pf->opt_wait_probe;
+    pf->opt_wait_probe = 0;
   }
   {
     ProfScope ps(&pf->prof, s, AMCL_PROF_CLOUD_WEIGHT);
@@ -759,6 +761,11 @@ extern "C" int amcl_pf_set_option(amcl_pf_t pf, int option, int64_t value)
     case AMCL_OPT_SEED:
       pf->seed = static_cast<uint64_t>(value);
       pf->step = 0;
+      return AMCL_OK;
+    case AMCL_OPT_WAIT_PROBE:
+      if (value < 0 || value > 1)
+        return fail(AMCL_EINVAL, "AMCL_OPT_WAIT_PROBE: 0 or 1");
+      pf->opt_wait_probe = static_cast<int>(value);
       return AMCL_OK;
     default:
       return fail(AMCL_ENOTSUP, "amcl_pf_set_option: unknown option");

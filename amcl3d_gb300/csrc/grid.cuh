@@ -53,6 +53,7 @@ struct WeightArgs
   int yaw_only;   // set by launch_cloud_weight when roll = pitch = 0
   float* scratch;           // two-phase only: ceil(P/32)*32*N floats
   uint64_t scratch_floats;  // capacity
+  int wait_probe;           // two-phase only: make one bounded wait give up (AMCL_OPT_WAIT_PROBE)
 };
 int launch_cloud_weight(amcl_grid_s* g, const WeightArgs& a, cudaStream_t s);
 // Chooses the kernel for AMCL_OPT_WEIGHT_KERNEL = 0.

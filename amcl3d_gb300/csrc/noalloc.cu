@@ -74,15 +74,20 @@ extern "C" int amcl_grid_cloud_weights_noalloc(amcl_grid_t g, const void* poses_
   if (two_phase_scratch_floats(P, n) > NOALLOC_MAX_SCRATCH_FLOATS)
     return fail(AMCL_ERANGE,
                 "amcl_grid_cloud_weights_noalloc: ceil(P/32)*32*N exceeds the 4194304-float (16 MiB) scratch array");
-  if (!g->built)
-    return fail(AMCL_ESTATE, "amcl_grid_cloud_weights_noalloc: grid not built");
   if (!P)
     return AMCL_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!g->built)
+  {
+    // computeCloudWeight of a grid never opened is 0 (Grid3d.cpp:136-137)
+    AMCL_CUDA_TRY(cudaMemsetAsync(out_dev, 0, P * sizeof(float), s));
+    AMCL_CUDA_TRY(cudaStreamSynchronize(s));
+    return AMCL_OK;
+  }
   float* base = nullptr;
   int rc = noalloc_base(&base);
   if (rc)
     return rc;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
   int* err = reinterpret_cast<int*>(base);
   AMCL_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));  // the error word starts at zero every call
   WeightArgs a{};

@@ -116,6 +116,7 @@ __global__ __launch_bounds__(32) void k_weight_tile_reduce(WeightArgs a, GridVie
   extern __shared__ __align__(16) unsigned char smem[];
   float* s_buf = reinterpret_cast<float*>(smem);  // TR_STAGES x TR_STAGE_PTS x 32
   __shared__ __align__(8) uint64_t s_bar[TR_STAGES];
+  __shared__ __align__(8) uint64_t s_probe;  // AMCL_OPT_WAIT_PROBE: a barrier nothing completes
   __shared__ float4 s_rg[MAX_RANGES];
   const int lane = threadIdx.x;
   const uint32_t tile = blockIdx.x;
@@ -129,15 +130,20 @@ __global__ __launch_bounds__(32) void k_weight_tile_reduce(WeightArgs a, GridVie
   const bool inm = active && (a.ignore_map || into_map(g, pose.x, pose.y, pose.z));
   const bool any = __any_sync(0xFFFFFFFFu, inm);
   if (lane == 0)
+  {
     for (int s = 0; s < TR_STAGES; ++s)
       mbar_init(&s_bar[s], 1);
+    mbar_init(&s_probe, 1);
+  }
   mbar_fence_init();
   __syncwarp();
   const float* slab = a.scratch + static_cast<uint64_t>(tile) * a.N * 32;
   const uint32_t nst = (a.N + TR_STAGE_PTS - 1) / TR_STAGE_PTS;
   CloudSum<SUM> acc;
-  bool ok = true;
-  if (any && a.N)
+  // The wait probe gives up (short budget) before any copy is issued, so the kernel
+  // leaves with nothing in flight; it exercises the error path of the bounded waits.
+  bool ok = a.wait_probe ? __all_sync(0xFFFFFFFFu, mbar_wait_bounded(&s_probe, 0, a.err, 1024u)) : true;
+  if (ok && any && a.N)
   {
     if (lane == 0)
       for (uint32_t st = 0; st < min(nst, static_cast<uint32_t>(TR_STAGES)); ++st)
@@ -147,13 +153,16 @@ __global__ __launch_bounds__(32) void k_weight_tile_reduce(WeightArgs a, GridVie
         bulk_g2s(s_buf + st * TR_STAGE_PTS * 32, slab + static_cast<uint64_t>(st) * TR_STAGE_PTS * 32, pts * 128u,
                  &s_bar[st]);
       }
+    uint32_t failed = 0;
     for (uint32_t st = 0; st < nst; ++st)
     {
       const int slot = st % TR_STAGES;
       const uint32_t parity = (st / TR_STAGES) & 1u;
-      if (!mbar_wait_bounded(&s_bar[slot], parity, a.err))
+      // every lane leaves together if any lane's wait gave up (the loop holds warp syncs)
+      if (!__all_sync(0xFFFFFFFFu, mbar_wait_bounded(&s_bar[slot], parity, a.err)))
       {
         ok = false;
+        failed = st;
         break;
       }
       const uint32_t pts = min(static_cast<uint32_t>(TR_STAGE_PTS), a.N - st * TR_STAGE_PTS);
@@ -179,9 +188,12 @@ __global__ __launch_bounds__(32) void k_weight_tile_reduce(WeightArgs a, GridVie
     }
     if (!ok)
     {
-      // Drain whatever is still in flight (bounded) before leaving.
-      for (uint32_t st = 0; st < min(nst, static_cast<uint32_t>(TR_STAGES)); ++st)
-        mbar_wait_bounded(&s_bar[st], 0, nullptr);
+      // Drain what is still in flight (bounded) before leaving: the wait gave up at
+      // stage `failed`, when stages [failed, issued) had been issued; stage j lands on
+      // slot j % TR_STAGES in the phase of parity (j / TR_STAGES) & 1.
+      const uint32_t issued = min(nst, failed + static_cast<uint32_t>(TR_STAGES));
+      for (uint32_t j = failed; j < issued; ++j)
+        mbar_wait_bounded(&s_bar[j % TR_STAGES], (j / TR_STAGES) & 1u, nullptr);
     }
   }
   float wpv = 0.0f, wrv = 0.0f;
@@ -217,15 +229,16 @@ int launch_fused(const WeightArgs& a, const GridView& g, cudaStream_t s)
 {
   const size_t smem = WT_CHUNK * sizeof(float4) + MAX_RANGES * sizeof(float4) + 2 * (WT_THREADS / 32) * sizeof(X320) +
                       (a.N && tables_staged(g) ? table_bytes(g) : 0);
-  static bool attr_done = false;
-  if (!attr_done)
-  {
-    cudaFuncSetAttribute(k_weight_fused<STORAGE, SUM, TAB_SHARED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         200 * 1024);
-    cudaFuncSetAttribute(k_weight_fused<STORAGE, SUM, TAB_GLOBAL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         200 * 1024);
-    attr_done = true;
-  }
+  static std::atomic<uint64_t> attr_done{ 0 };
+  const int rc = once_per_device(attr_done, [] {
+    AMCL_CUDA_TRY(cudaFuncSetAttribute(k_weight_fused<STORAGE, SUM, TAB_SHARED>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    AMCL_CUDA_TRY(cudaFuncSetAttribute(k_weight_fused<STORAGE, SUM, TAB_GLOBAL>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    return static_cast<int>(AMCL_OK);
+  });
+  if (rc)
+    return rc;
   if (tables_staged(g))
     k_weight_fused<STORAGE, SUM, TAB_SHARED><<<ceil_div(a.P, WT_THREADS), WT_THREADS, smem, s>>>(a, g);
   else
@@ -239,13 +252,16 @@ int launch_two_phase(const WeightArgs& a, const GridView& g, cudaStream_t s)
 {
   const size_t smem1 = TP_PTS_PER_BLOCK * sizeof(float4) + 32 * sizeof(PartRec) + (tables_staged(g) ? table_bytes(g) : 0);
   const size_t smem2 = static_cast<size_t>(TR_STAGES) * TR_STAGE_PTS * 32 * sizeof(float);
-  static bool attr_done = false;
-  if (!attr_done)
-  {
-    cudaFuncSetAttribute(k_weight_tile_vals<STORAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(k_weight_tile_reduce<SUM>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr_done = true;
-  }
+  static std::atomic<uint64_t> attr_done{ 0 };
+  const int rc = once_per_device(attr_done, [] {
+    AMCL_CUDA_TRY(
+        cudaFuncSetAttribute(k_weight_tile_vals<STORAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    AMCL_CUDA_TRY(
+        cudaFuncSetAttribute(k_weight_tile_reduce<SUM>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    return static_cast<int>(AMCL_OK);
+  });
+  if (rc)
+    return rc;
   const unsigned tiles = ceil_div(a.P, 32);
   if (a.N)
   {

@@ -124,8 +124,9 @@ int amcl_grid_cloud_weights(amcl_grid_t g, const float* poses4, uint32_t P, cons
  * nothing is allocated; the two-phase kernel's scratch is a fixed 16 MiB
  * file-scope device array that every GPU loading the library holds until exit.
  * poses (P x float4 x, y, z, yaw) and cloud (n x float4 x, y, z, unused) are
- * 16-byte aligned device buffers, out is P device floats; the call runs on `stream`
- * (NULL: the default stream) and synchronises it.  Limits: P <= 65536 and
+ * 16-byte aligned device buffers, out is P device floats (all 0 when no grid is
+ * built, as amcl_grid_cloud_weights gives); the call runs on `stream` (NULL: the
+ * default stream) and waits for that stream to finish before it returns.  Limits: P <= 65536 and
  * ceil(P/32)*32*n <= 4194304, else AMCL_ERANGE.  All calls share the array, so calls
  * that overlap on the GPU race.  The first call on a device looks the array's
  * address up; make it before any stream capture. */
@@ -221,7 +222,12 @@ enum
    * sums from a device scratch buffer). */
   AMCL_OPT_WEIGHT_KERNEL = 3,
   /* Seed of the counter-based generator (resets its counter). */
-  AMCL_OPT_SEED = 4
+  AMCL_OPT_SEED = 4,
+  /* Test of the bounded device-side waits: 1 = the next update's two-phase weighting
+   * waits on a barrier that nothing completes, gives up after a short budget (before
+   * it issues any copy) and weighs nothing; the update's result is then reported as
+   * AMCL_ETIMEDOUT by the next call that reads the filter back.  One use, then 0. */
+  AMCL_OPT_WAIT_PROBE = 5
 };
 int amcl_pf_set_option(amcl_pf_t pf, int option, int64_t value);
 

@@ -9,6 +9,7 @@ import ctypes as C
 import numpy as np
 import pytest
 
+import oracle as O
 from conftest import small_grid_data
 
 pytestmark = pytest.mark.gpu
@@ -50,6 +51,8 @@ def test_noalloc_matches_allocating_entry_point(amcl, ref_small):
         got = d_out.cpu().numpy()
         want = G.computeCloudWeights(poses, cloud, roll, pitch)
         np.testing.assert_array_equal(got, want)  # same kernels, same bits
+        # and the oracle's computeCloudWeight directly (the GPU's sin/cos: yaw_trig=1)
+        np.testing.assert_array_equal(got, O.cloud_weights(g, poses, cloud, roll, pitch, yaw_trig=1))
         results.append(got)
     assert not np.array_equal(results[0], results[1])
     assert free[0] == free[1]  # no device memory taken between the calls
@@ -67,3 +70,19 @@ def test_noalloc_rejects_sizes_beyond_the_array(amcl, ref_small):
     assert b"65536" in N.lib.amcl_last_error()
     assert _noalloc(N, G, fake, 4096, fake, 1025, fake) == 7  # 4096*1025 > 4194304
     assert b"scratch" in N.lib.amcl_last_error()
+
+
+def test_noalloc_unbuilt_grid_gives_zeros(amcl):
+    """computeCloudWeight of a grid that was never opened is 0 (Grid3d.cpp:136-137)."""
+    import torch
+
+    from amcl3d_gb300 import _native as N
+
+    G = amcl.Grid3d()
+    dev = torch.device("cuda", 0)
+    poses = torch.zeros((5, 4), dtype=torch.float32, device=dev)
+    cloud = torch.zeros((20, 4), dtype=torch.float32, device=dev)
+    out = torch.full((5,), -7.0, dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+    assert _noalloc(N, G, poses.data_ptr(), 5, cloud.data_ptr(), 20, out.data_ptr()) == 0
+    assert np.all(out.cpu().numpy() == 0.0)
