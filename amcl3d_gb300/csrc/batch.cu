@@ -127,7 +127,7 @@ __global__ __launch_bounds__(NT) void k_b_predict(BatchDev d)
   }
 }
 
-template <int STORAGE, int SUM, int TAB>
+template <int STORAGE, int SUM, int TAB, int FS>
 __device__ __forceinline__ void b_weigh(const BatchDev& d, const SlotStep& st, const GridView& g, uint32_t tile,
                                         uint32_t chunk, float4* s_pts, const float4* s_rg, X320* s_part,
                                         const float2* s_tab)
@@ -150,7 +150,7 @@ __device__ __forceinline__ void b_weigh(const BatchDev& d, const SlotStep& st, c
   a.acc_wp = d.acc + static_cast<uint64_t>(st.slot) * ACC_WORDS + ACC_WP * NDIG;
   a.acc_wr = d.acc + static_cast<uint64_t>(st.slot) * ACC_WORDS + ACC_WR * NDIG;
   a.yaw_only = st.yaw_only;
-  weigh_block<STORAGE, SUM, TAB>(a, g, tile * blockDim.x, chunk, s_pts, s_rg, s_part, s_tab);
+  weigh_block<STORAGE, SUM, TAB, FS>(a, g, tile * blockDim.x, chunk, s_pts, s_rg, s_part, s_tab);
 }
 
 // Persistent: blocks take (filter, particle tile) items of one fused queue until it is
@@ -172,7 +172,8 @@ constexpr int COUNT_WORDS = SQ_BASE + 2 * N_CLASSES;
 __host__ __device__ inline int weight_class(int storage, int cloud_sum) { return storage * 2 + (cloud_sum ? 1 : 0); }
 __host__ __device__ inline int fused_queue(int cls, int gslot) { return cls * N_GSLOTS + (gslot < 0 ? BATCH_GRIDS : gslot); }
 
-template <int STORAGE, int SUM, bool PG, int MAXT>
+// FS: the slot grid has floor constants (only with PG; set by the launcher).
+template <int STORAGE, int SUM, bool PG, int MAXT, int FS = 0>
 __global__ __launch_bounds__(MAXT, MAXT >= 512 ? 1 : 3) void k_b_weight(BatchDev d, GridView gp, uint32_t q,
                                                                          uint32_t chunk)
 {
@@ -208,7 +209,7 @@ __global__ __launch_bounds__(MAXT, MAXT >= 512 ? 1 : 3) void k_b_weight(BatchDev
         s_loaded = static_cast<int>(wi.x);
     }
     // slot grids always have staged tables (assign_grid_slots); descriptor grids may not
-    b_weigh<STORAGE, SUM, PG ? TAB_SHARED : TAB_EITHER>(d, st, PG ? gp : st.g, wi.y, chunk, s_pts, s_rg, s_part,
+    b_weigh<STORAGE, SUM, PG ? TAB_SHARED : TAB_EITHER, FS>(d, st, PG ? gp : st.g, wi.y, chunk, s_pts, s_rg, s_part,
                                                         s_tab);
   }
 }
@@ -631,11 +632,15 @@ int launch_fused_class(amcl_batch_s* b, const BatchDev& d, int threads, uint32_t
     int per_sm = 0;
     if (slot < BATCH_GRIDS)
     {
-      AMCL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_b_weight<STORAGE, SUM, true, MAXT>,
-                                                                  threads, smem));
+      const GridView& gv = b->gset.g[slot];
+      AMCL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &per_sm, gv.fast_idx ? k_b_weight<STORAGE, SUM, true, MAXT, 1> : k_b_weight<STORAGE, SUM, true, MAXT, 0>,
+          threads, smem));
       const unsigned grid = static_cast<unsigned>(device_sm_count() * std::max(per_sm, 1));
-      k_b_weight<STORAGE, SUM, true, MAXT><<<grid, threads, smem, s>>>(d, b->gset.g[slot], static_cast<uint32_t>(q),
-                                                                        chunk);
+      if (gv.fast_idx)
+        k_b_weight<STORAGE, SUM, true, MAXT, 1><<<grid, threads, smem, s>>>(d, gv, static_cast<uint32_t>(q), chunk);
+      else
+        k_b_weight<STORAGE, SUM, true, MAXT, 0><<<grid, threads, smem, s>>>(d, gv, static_cast<uint32_t>(q), chunk);
     }
     else
     {
@@ -707,7 +712,9 @@ int fused_smem_attr(size_t smem)
   if ((rc = smem_attr(k_b_weight<STORAGE, SUM, true, 256>, smem)) ||
       (rc = smem_attr(k_b_weight<STORAGE, SUM, false, 256>, smem)) ||
       (rc = smem_attr(k_b_weight<STORAGE, SUM, true, 512>, smem)) ||
-      (rc = smem_attr(k_b_weight<STORAGE, SUM, false, 512>, smem)))
+      (rc = smem_attr(k_b_weight<STORAGE, SUM, false, 512>, smem)) ||
+      (rc = smem_attr(k_b_weight<STORAGE, SUM, true, 256, 1>, smem)) ||
+      (rc = smem_attr(k_b_weight<STORAGE, SUM, true, 512, 1>, smem)))
     return rc;
   return AMCL_OK;
 }

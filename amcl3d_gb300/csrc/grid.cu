@@ -55,6 +55,43 @@ static float table_threshold(double res, uint32_t k)
   return x;
 }
 
+// Floor constants mag[a] = 2^23 + m[a] of the hot loop: with B = bits(2^23) =
+// 0x4B000000 the index sum_a (B + m[a] + k[a]) * stride[a] equals
+// sum_a k[a] * stride[a] (mod 2^32) when sum_a m[a] * stride[a] = R = -B * (1 + sy + sz);
+// R is written in the mixed radix of the strides (m2 = R / sz, m1 = (R % sz) / sy,
+// m0 = R % sy).  Each m[a] must leave room for the floors of a valid coordinate (up to
+// size + 1 cells below 2^23 past the constant), which holds whenever
+// size_x * size_y >= 1024 and every axis is below 2^22 cells.
+static void grid_floor_constants(GridView& v)
+{
+  const uint64_t two32 = 1ull << 32;
+  const uint64_t sy = v.step_y, sz = v.step_z;
+  v.fast_idx = 0;
+  v.pad_cell = 0;
+  for (int a = 0; a < 3; ++a)
+    v.mag[a] = 12582912.0f;
+  if (v.cells == 0 || v.cells >= two32 - 1 || sy == 0 || sz == 0 || sz >= two32)
+    return;
+  const uint64_t B = 0x4B000000ull;
+  const uint64_t R = (two32 - (B * ((1 + sy + sz) % two32)) % two32) % two32;
+  const uint64_t m2 = R / sz, r2 = R % sz;
+  const uint64_t m1 = r2 / sy, m0 = r2 % sy;
+  const uint64_t m[3] = { m0, m1, m2 };
+  for (int a = 0; a < 3; ++a)
+    if (m[a] + v.size[a] + 2 > (1ull << 23))
+      return;
+  uint64_t chk = 0;
+  const uint64_t stride[3] = { 1, sy, sz };
+  for (int a = 0; a < 3; ++a)
+    chk = (chk + ((B + m[a]) % two32) * stride[a]) % two32;
+  if (chk != 0)
+    return;
+  for (int a = 0; a < 3; ++a)
+    v.mag[a] = static_cast<float>(8388608.0 + static_cast<double>(m[a]));
+  v.pad_cell = static_cast<uint32_t>(v.cells);
+  v.fast_idx = 1;
+}
+
 size_t grid_table_floats(const amcl_grid_s* g)
 {
   return static_cast<size_t>(g->info.size[0]) + g->info.size[1] + g->info.size[2] + 3;
@@ -95,6 +132,7 @@ int grid_prepare_view(amcl_grid_s* g)
   v.step_y = in.size[0];
   v.step_z = in.size[0] * in.size[1];
   v.cells = g->cells();
+  grid_floor_constants(v);
   // Pairs (T[k], T[k+1]) per axis, T[size+1] = +inf: one 64-bit load settles a cell.
   std::vector<float2> pairs(g->tabs_host.size());
   for (int a = 0; a < 3; ++a)
@@ -568,12 +606,13 @@ extern "C" int amcl_grid_build(amcl_grid_t g, const float* xyz, uint64_t n, uint
     return rc;
   const uint64_t cells = g->cells();
   cudaStream_t s = g->st.s;
-  if ((rc = g->dist.ensure(cells * 4)) || (rc = g->prob.ensure(cells * 4)))
+  if ((rc = g->dist.ensure(cells * 4)) || (rc = g->prob.ensure((cells + 1) * 4)))
     return rc;
   g->prob16.release();
   g->prob8.release();
   g->info.storage = AMCL_GRID_F32;
   g->info.u8_scale = 0.0f;
+  AMCL_CUDA_TRY(cudaMemsetAsync(g->prob.as<float>() + cells, 0, 4, s));  // the zero pad cell
 
   // Query coordinates (float)(min + i*res) per axis (PointCloudTools.cpp:127-129).
   std::vector<float> q[3];
@@ -652,12 +691,13 @@ extern "C" int amcl_grid_load_cells(amcl_grid_t g, const amcl_grid_info* info, c
     if (info->size[a] != g->info.size[a])
       return fail(AMCL_EINVAL, "amcl_grid_load_cells: sizes do not match ceil((max-min)/res)");
   const uint64_t cells = g->cells();
-  if ((rc = g->dist.ensure(cells * 4)) || (rc = g->prob.ensure(cells * 4)))
+  if ((rc = g->dist.ensure(cells * 4)) || (rc = g->prob.ensure((cells + 1) * 4)))
     return rc;
   g->prob16.release();
   g->prob8.release();
   g->info.storage = AMCL_GRID_F32;
   g->info.u8_scale = 0.0f;
+  AMCL_CUDA_TRY(cudaMemsetAsync(g->prob.as<float>() + cells, 0, 4, g->st.s));  // the zero pad cell
   if (dist)
     AMCL_CUDA_TRY(cudaMemcpyAsync(g->dist.p, dist, cells * 4, cudaMemcpyHostToDevice, g->st.s));
   else
@@ -706,15 +746,17 @@ extern "C" int amcl_grid_set_storage(amcl_grid_t g, int storage)
   int rc;
   if (storage == AMCL_GRID_F16 && !g->prob16.p)
   {
-    if ((rc = g->prob16.ensure(cells * 2)))
+    if ((rc = g->prob16.ensure((cells + 1) * 2)))
       return rc;
+    AMCL_CUDA_TRY(cudaMemsetAsync(g->prob16.as<__half>() + cells, 0, 2, s));
     k_quantize<<<nb, 256, 0, s>>>(g->prob.as<float>(), cells, g->prob16.as<__half>(), nullptr, 0.0f);
     AMCL_LAUNCH_CHECK("k_quantize(f16)");
   }
   if (storage == AMCL_GRID_U8 && !g->prob8.p)
   {
-    if ((rc = g->prob8.ensure(cells)))
+    if ((rc = g->prob8.ensure(cells + 1)))
       return rc;
+    AMCL_CUDA_TRY(cudaMemsetAsync(g->prob8.as<uint8_t>() + cells, 0, 1, s));
     DevBuf mbits;
     if ((rc = mbits.ensure(4)))
       return rc;

@@ -58,6 +58,13 @@ struct GridView
   double min[3];
   uint64_t cells;
   int built;
+  // Floor constants of the yaw-only loop: mag[a] = 2^23 + m[a] with
+  // sum_a bits(mag[a]) * stride[a] = 0 (mod 2^32), strides (1, step_y, step_z), so the
+  // bits of fma_rd(X[a], inv_lo[a], mag[a]) = bits(mag[a]) + floor(X[a] * inv_lo[a]),
+  // weighted by the strides, sum to the cell index itself with no bias to remove.
+  float mag[3];
+  uint32_t pad_cell;  // index of the zero cell stored after the last cell of every prob array
+  int fast_idx;       // mag[] exists and pad_cell < 2^32
 };
 
 // Per-particle constants of the transform.

@@ -32,7 +32,7 @@ namespace
 constexpr int WT_THREADS = 192;  // 6 warps; 4 blocks per SM by registers (80 per thread)
 constexpr int WT_CHUNK = 1024;  // points staged per block iteration (16 KB)
 
-template <int STORAGE, int SUM, int TAB>
+template <int STORAGE, int SUM, int TAB, int FS = 0>
 __global__ __launch_bounds__(WT_THREADS, 4) void k_weight_fused(WeightArgs a, GridView g)
 {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -45,7 +45,7 @@ __global__ __launch_bounds__(WT_THREADS, 4) void k_weight_fused(WeightArgs a, Gr
     load_tables(g, s_tab);
   for (uint32_t i = threadIdx.x; i < a.nr; i += blockDim.x)
     s_rg[i] = a.ranges[i];
-  weigh_block<STORAGE, SUM, TAB>(a, g, blockIdx.x * blockDim.x, WT_CHUNK, s_pts, s_rg, s_part, s_tab);
+  weigh_block<STORAGE, SUM, TAB, FS>(a, g, blockIdx.x * blockDim.x, WT_CHUNK, s_pts, s_rg, s_part, s_tab);
 }
 
 // ---- two-phase ----------------------------------------------------------------------------
@@ -235,11 +235,19 @@ int launch_fused(const WeightArgs& a, const GridView& g, cudaStream_t s)
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     AMCL_CUDA_TRY(cudaFuncSetAttribute(k_weight_fused<STORAGE, SUM, TAB_GLOBAL>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    AMCL_CUDA_TRY(cudaFuncSetAttribute(k_weight_fused<STORAGE, SUM, TAB_SHARED, 1>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    AMCL_CUDA_TRY(cudaFuncSetAttribute(k_weight_fused<STORAGE, SUM, TAB_GLOBAL, 1>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     return static_cast<int>(AMCL_OK);
   });
   if (rc)
     return rc;
-  if (tables_staged(g))
+  if (g.fast_idx && tables_staged(g))
+    k_weight_fused<STORAGE, SUM, TAB_SHARED, 1><<<ceil_div(a.P, WT_THREADS), WT_THREADS, smem, s>>>(a, g);
+  else if (g.fast_idx)
+    k_weight_fused<STORAGE, SUM, TAB_GLOBAL, 1><<<ceil_div(a.P, WT_THREADS), WT_THREADS, smem, s>>>(a, g);
+  else if (tables_staged(g))
     k_weight_fused<STORAGE, SUM, TAB_SHARED><<<ceil_div(a.P, WT_THREADS), WT_THREADS, smem, s>>>(a, g);
   else
     k_weight_fused<STORAGE, SUM, TAB_GLOBAL><<<ceil_div(a.P, WT_THREADS), WT_THREADS, smem, s>>>(a, g);

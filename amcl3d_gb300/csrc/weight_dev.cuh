@@ -52,6 +52,13 @@ struct CloudSum
     }
     n += 1;
   }
+  // The compensated add without the count (the loops with floor constants count apart).
+  __device__ __forceinline__ void add_uncounted(float v)
+  {
+    const float t = fadd(sum, v);
+    comp = fadd(comp, fabsf(sum) >= fabsf(v) ? fadd(fsub(sum, t), v) : fadd(fsub(v, t), sum));
+    sum = t;
+  }
   // Grid3d.cpp:198: 0 with 10 or fewer points, else the mean.
   __device__ __forceinline__ float weight() const
   {
@@ -120,6 +127,83 @@ __device__ __forceinline__ void weigh_chunk_yaw2(const float4* s_pts, const floa
     for (int j = 0; j < YAW_UNROLL; ++j)
       if (cell[j] != 0xFFFFFFFFu)
         acc.add(v[j]);
+  }
+}
+
+// ---- yaw-only loop with the grid's floor constants (GridView::fast_idx) -------------------
+// The cheaper form of weigh_chunk_yaw2: the floors use the constants mag[a], so the
+// bits of the round-down FMAs weighted by the strides are the cell index with nothing
+// to subtract; a rejected point gathers the zero cell stored after the grid (pad_cell)
+// and is not counted, and adding +0.0 to the running sum (never below +0) leaves it
+// unchanged, so the sum and the count are the reference's (Grid3d.cpp:185-195).
+
+// Cell of one point from its coordinates X and round-down floors lo, pad_cell when the
+// reference skips it; `near` marks floors that may be one cell off (the pair table
+// settles them).
+template <int TAB>
+__device__ __forceinline__ uint32_t settle_fast(const GridView& g, const float2* tab, float2 Xxy, float Xz, float2 loxy,
+                                                float loz, bool near, int& n)
+{
+  bool valid = (__float_as_uint(Xxy.x) < __float_as_uint(g.V[0])) &
+               (__float_as_uint(Xxy.y) < __float_as_uint(g.V[1])) & (__float_as_uint(Xz) < __float_as_uint(g.V[2]));
+  uint32_t idx = __float_as_uint(loxy.x) + __float_as_uint(loxy.y) * g.step_y + __float_as_uint(loz) * g.step_z;
+  if (near && valid)
+  {
+    const int kx = locate_pair<TAB>(Xxy.x, tab, g, 0);
+    const int ky = locate_pair<TAB>(Xxy.y, tab, g, 1);
+    const int kz = locate_pair<TAB>(Xz, tab, g, 2);
+    valid = (kx | ky | kz) >= 0;
+    idx = static_cast<uint32_t>(kx) + static_cast<uint32_t>(ky) * g.step_y + static_cast<uint32_t>(kz) * g.step_z;
+  }
+  n += valid ? 1 : 0;
+  return valid ? idx : g.pad_cell;
+}
+
+// One branch per point (the table settles a point near a cell boundary in place).
+template <int STORAGE, int SUM, int TAB>
+__device__ __forceinline__ void weigh_chunk_yaw2_fast(const float4* s_pts, const float* s_z, uint32_t cnt,
+                                                      const float2* s_tab, const GridView& g, const PartYaw2& q,
+                                                      CloudSum<SUM>& acc)
+{
+  const float2 mxy = make_float2(g.mag[0], g.mag[1]);
+  for (uint32_t k = 0; k < cnt; k += YAW_UNROLL)
+  {
+    float zs[YAW_UNROLL];
+#pragma unroll
+    for (int j = 0; j < YAW_UNROLL; j += 4)
+    {
+      const float4 z4 = *reinterpret_cast<const float4*>(s_z + k + j);
+      zs[j] = z4.x;
+      zs[j + 1] = z4.y;
+      zs[j + 2] = z4.z;
+      zs[j + 3] = z4.w;
+    }
+    uint32_t cell[YAW_UNROLL];
+#pragma unroll
+    for (int j = 0; j < YAW_UNROLL; ++j)
+    {
+      const float4 xxyy = s_pts[k + j];
+      const float2 s01 = __fadd2_rn(__ffma2_rn(make_float2(xxyy.x, xxyy.y), q.rx, q.nz),
+                                    __ffma2_rn(make_float2(xxyy.z, xxyy.w), q.ry, q.nz));
+      const float2 X01 = __fadd2_rn(s01, q.h);
+      const float2 lo = __ffma2_rd(X01, q.lo, mxy), hi = __ffma2_rd(X01, q.hi, mxy);
+      const float Xz = fadd(zs[j], q.hz);
+      const float loz = __fmaf_rd(Xz, q.loz, g.mag[2]), hiz = __fmaf_rd(Xz, q.hiz, g.mag[2]);
+      const bool near = !(lo.x == hi.x) | !(lo.y == hi.y) | !(loz == hiz);
+      cell[j] = settle_fast<TAB>(g, s_tab, X01, Xz, lo, loz, near, acc.n);
+    }
+    float v[YAW_UNROLL];
+#pragma unroll
+    for (int j = 0; j < YAW_UNROLL; ++j)
+      v[j] = gather_prob<STORAGE>(g, cell[j]);
+#pragma unroll
+    for (int j = 0; j < YAW_UNROLL; ++j)
+    {
+      if (SUM == 0)
+        acc.sum = fadd(acc.sum, v[j]);
+      else
+        acc.add_uncounted(v[j]);
+    }
   }
 }
 
@@ -230,12 +314,14 @@ __device__ __forceinline__ void load_tables(const GridView& g, float2* s_tab)
   }
 }
 
+// FS: the grid has floor constants (GridView::fast_idx, checked by the launcher), so the
+// yaw-only points take weigh_chunk_yaw2_fast.
 // One block of particles [p0, p0 + blockDim) of one filter, one thread per particle
 // over the whole cloud in cloud order (the fused weighting).  The caller has loaded
 // s_tab (when a.N > 0) and s_rg.  s_pts holds `chunk` float4 (a multiple of UNROLL):
 // as many points per stage, or 4/5 as many (a multiple of YAW_UNROLL) in the yaw-only
 // staging.  Every thread of the block must call this.
-template <int STORAGE, int SUM, int TAB>
+template <int STORAGE, int SUM, int TAB, int FS = 0>
 __device__ __forceinline__ void weigh_block(const WeightArgs& a, const GridView& g, uint32_t p0, uint32_t chunk,
                                             float4* s_pts, const float4* s_rg, X320* s_part, const float2* s_tab)
 {
@@ -286,7 +372,9 @@ __device__ __forceinline__ void weigh_block(const WeightArgs& a, const GridView&
     __syncthreads();
     if (!inm)
       continue;
-    if (mode == XF_YAW)
+    if (FS && mode == XF_YAW)
+      weigh_chunk_yaw2_fast<STORAGE, SUM, TAB>(s_pts, s_z, cnt8, s_tab, g, q, acc);
+    else if (mode == XF_YAW)
       weigh_chunk_yaw2<STORAGE, SUM, TAB>(s_pts, s_z, cnt8, s_tab, g, q, acc);
     else if (mode == XF_EXACT)
       weigh_chunk<STORAGE, SUM, XF_EXACT, false, TAB>(s_pts, s_z, cnt8, s_tab, g, xf, acc);
