@@ -828,6 +828,18 @@ void assign_grid_slots(amcl_batch_s* b, SlotStep* hs, const std::vector<const am
     hs[i].gslot = step_grid[i] && tables_staged(step_grid[i]->view) ? slot_of(step_grid[i]) : -1;
 }
 
+// Grows a device or pinned buffer to at least `need` bytes, at least doubling (up to
+// `cap`): a workload that creeps upwards reallocates, and so frees (a device-wide
+// synchronisation) and drops the captured graphs, only a few times.
+template <typename Buf>
+int grow(Buf& buf, size_t need, size_t cap = SIZE_MAX)
+{
+  if (buf.p && need <= buf.bytes)
+    return AMCL_OK;
+  const size_t dbl = std::max<size_t>(2 * buf.bytes, 1u << 20);
+  return buf.ensure(std::max(need, std::min(dbl, cap)));
+}
+
 // Weighting work items of the packed steps.  Fused steps: (step, particle tile of
 // `threads`), grouped by fused queue ((storage, sum) class and grid slot), longest
 // scans first within a queue (stable, so a filter's tiles stay adjacent and reuse the
@@ -871,6 +883,18 @@ void build_weight_items(amcl_batch_s* b, int threads)
     hcnt[w + 1] = k;
     if (n)
       mask |= 1ull << (split ? SPLIT_MASK_SHIFT + (qi - N_FUSED_Q) : qi);
+  }
+  // Every grid slot of a fused class with work is launched (a slot without items returns
+  // at once), so the captured graph depends on the classes present rather than on which
+  // maps this step's filters happen to use: fewer graphs to build while serving.
+  for (int cls = 0; cls < N_CLASSES; ++cls)
+  {
+    bool any = false;
+    for (int j = 0; j < N_GSLOTS; ++j)
+      any |= (mask >> fused_queue(cls, j < BATCH_GRIDS ? j : -1)) & 1u;
+    if (any)
+      for (int j = 0; j < BATCH_GRIDS; ++j)
+        mask |= 1ull << fused_queue(cls, j);
   }
   b->n_wt = k;
   b->class_mask = mask;
@@ -929,8 +953,8 @@ int plan_split(amcl_batch_s* b, int threads)
   const void* old[3] = { b->xf.p, b->scratch.p, b->tile_done.p };
   const size_t old_tiles = b->tile_done.bytes;
   int rc;
-  if ((rc = b->xf.ensure(xo * sizeof(SplitRec))) || (rc = b->scratch.ensure(sc * 4)) ||
-      (rc = b->tile_done.ensure(tiles * 4)))
+  if ((rc = grow(b->xf, xo * sizeof(SplitRec))) || (rc = grow(b->scratch, sc * 4, b->scratch_cap)) ||
+      (rc = grow(b->tile_done, tiles * 4)))
     return rc;
   if (b->tile_done.bytes != old_tiles || b->tile_done.p != old[2])
     AMCL_CUDA_TRY(cudaMemsetAsync(b->tile_done.p, 0, b->tile_done.bytes, b->st.s));
@@ -1050,7 +1074,7 @@ int pack_steps(amcl_batch_s* b)
   if (items * sizeof(uint2) > b->wt_items.bytes)
   {
     b->drop_graphs();
-    if ((rc = b->wt_items.ensure(items * sizeof(uint2))) || (rc = b->h_wt.ensure(items * sizeof(uint2))))
+    if ((rc = grow(b->wt_items, items * sizeof(uint2))) || (rc = grow(b->h_wt, items * sizeof(uint2))))
       return rc;
   }
   build_weight_items(b, threads);

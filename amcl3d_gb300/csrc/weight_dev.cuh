@@ -9,6 +9,7 @@ namespace amcl
 {
 constexpr int UNROLL = 8;
 constexpr int YAW_UNROLL = 8;  // points per group of the paired yaw-only loop
+constexpr int FAST_UNROLL = 8;  // points per group of the loop with floor constants
 constexpr int MAX_RANGES = 64;
 
 __device__ __forceinline__ float exp_f32_via_f64(float x) { return __double2float_rn(exp(static_cast<double>(x))); }
@@ -160,17 +161,17 @@ __device__ __forceinline__ uint32_t settle_fast(const GridView& g, const float2*
 }
 
 // One branch per point (the table settles a point near a cell boundary in place).
-template <int STORAGE, int SUM, int TAB>
+template <int STORAGE, int SUM, int TAB, int U = FAST_UNROLL>
 __device__ __forceinline__ void weigh_chunk_yaw2_fast(const float4* s_pts, const float* s_z, uint32_t cnt,
                                                       const float2* s_tab, const GridView& g, const PartYaw2& q,
                                                       CloudSum<SUM>& acc)
 {
   const float2 mxy = make_float2(g.mag[0], g.mag[1]);
-  for (uint32_t k = 0; k < cnt; k += YAW_UNROLL)
+  for (uint32_t k = 0; k < cnt; k += U)
   {
-    float zs[YAW_UNROLL];
+    float zs[U];
 #pragma unroll
-    for (int j = 0; j < YAW_UNROLL; j += 4)
+    for (int j = 0; j < U; j += 4)
     {
       const float4 z4 = *reinterpret_cast<const float4*>(s_z + k + j);
       zs[j] = z4.x;
@@ -178,9 +179,9 @@ __device__ __forceinline__ void weigh_chunk_yaw2_fast(const float4* s_pts, const
       zs[j + 2] = z4.z;
       zs[j + 3] = z4.w;
     }
-    uint32_t cell[YAW_UNROLL];
+    uint32_t cell[U];
 #pragma unroll
-    for (int j = 0; j < YAW_UNROLL; ++j)
+    for (int j = 0; j < U; ++j)
     {
       const float4 xxyy = s_pts[k + j];
       const float2 s01 = __fadd2_rn(__ffma2_rn(make_float2(xxyy.x, xxyy.y), q.rx, q.nz),
@@ -192,12 +193,12 @@ __device__ __forceinline__ void weigh_chunk_yaw2_fast(const float4* s_pts, const
       const bool near = !(lo.x == hi.x) | !(lo.y == hi.y) | !(loz == hiz);
       cell[j] = settle_fast<TAB>(g, s_tab, X01, Xz, lo, loz, near, acc.n);
     }
-    float v[YAW_UNROLL];
+    float v[U];
 #pragma unroll
-    for (int j = 0; j < YAW_UNROLL; ++j)
+    for (int j = 0; j < U; ++j)
       v[j] = gather_prob<STORAGE>(g, cell[j]);
 #pragma unroll
-    for (int j = 0; j < YAW_UNROLL; ++j)
+    for (int j = 0; j < U; ++j)
     {
       if (SUM == 0)
         acc.sum = fadd(acc.sum, v[j]);
@@ -321,7 +322,7 @@ __device__ __forceinline__ void load_tables(const GridView& g, float2* s_tab)
 // s_tab (when a.N > 0) and s_rg.  s_pts holds `chunk` float4 (a multiple of UNROLL):
 // as many points per stage, or 4/5 as many (a multiple of YAW_UNROLL) in the yaw-only
 // staging.  Every thread of the block must call this.
-template <int STORAGE, int SUM, int TAB, int FS = 0>
+template <int STORAGE, int SUM, int TAB, int FS = 0, int U = FAST_UNROLL>
 __device__ __forceinline__ void weigh_block(const WeightArgs& a, const GridView& g, uint32_t p0, uint32_t chunk,
                                             float4* s_pts, const float4* s_rg, X320* s_part, const float2* s_tab)
 {
@@ -373,7 +374,7 @@ __device__ __forceinline__ void weigh_block(const WeightArgs& a, const GridView&
     if (!inm)
       continue;
     if (FS && mode == XF_YAW)
-      weigh_chunk_yaw2_fast<STORAGE, SUM, TAB>(s_pts, s_z, cnt8, s_tab, g, q, acc);
+      weigh_chunk_yaw2_fast<STORAGE, SUM, TAB, U>(s_pts, s_z, cnt8, s_tab, g, q, acc);
     else if (mode == XF_YAW)
       weigh_chunk_yaw2<STORAGE, SUM, TAB>(s_pts, s_z, cnt8, s_tab, g, q, acc);
     else if (mode == XF_EXACT)

@@ -134,8 +134,14 @@ def make_scan_pool(maps, seed, n_max_points, per_map=4):
 
 
 def run_load(server: Server, grids, pools, n_sessions: int, rate_hz: float, duration_s: float, churn_per_s: float,
-             p_range=(1000, 100000), n_range=(500, 10000), seed=0, warmup_s=1.0, odom=None, max_queue=4):
-    """Open-loop Poisson load; returns latency percentiles and aggregate throughput."""
+             p_range=(1000, 100000), n_range=(500, 10000), seed=0, warmup_s=1.0, odom=None, max_queue=None):
+    """Open-loop Poisson load; returns latency percentiles and aggregate throughput.
+
+    A request's latency runs from its scheduled arrival time (not from when this loop
+    got round to submitting it) to its result being ready, so a load generator that
+    falls behind cannot hide queueing.  max_queue=None serves every scan; an integer
+    skips a scan arriving while that many of the session's requests are waiting, as a
+    node whose filter is busy does, and counts it in dropped_behind."""
     from . import synth as S
 
     rng = np.random.default_rng(seed)
@@ -191,8 +197,8 @@ def run_load(server: Server, grids, pools, n_sessions: int, rate_hz: float, dura
                 continue
             per_session[sid] = per_session.get(sid, 1) - 1
             if td >= t_meas and status == 0:
-                lat.append(td - ts)
-                weights += info
+                lat.append(td - info[1])
+                weights += info[0]
                 done_req += 1
         # churn: one session leaves, a new one arrives (waiting for admission)
         if now >= next_churn and specs:
@@ -211,18 +217,18 @@ def run_load(server: Server, grids, pools, n_sessions: int, rate_hz: float, dura
             heapq.heappush(events, (now + rng.exponential(1.0 / rate_hz), 0, sid))
         # arrivals
         while events and events[0][0] <= now:
-            _, _, sid = heapq.heappop(events)
+            t_arr, _, sid = heapq.heappop(events)
             if sid not in specs:
                 continue
             spec, scan, rg = specs[sid]
-            if per_session.get(sid, 0) >= max_queue:
+            if max_queue is not None and per_session.get(sid, 0) >= max_queue:
                 dropped += 1  # the session is that far behind: skip this scan, as the node's threshold gating does
             else:
                 ticket = server.submit(sid, scan, rg, odom, 0.5, 0.1, 0.0, 0.0, True)
-                outstanding[ticket] = spec.P * scan.shape[0]
+                outstanding[ticket] = (spec.P * scan.shape[0], t_arr)
                 per_session[sid] = per_session.get(sid, 0) + 1
                 submitted += 1
-            heapq.heappush(events, (now + rng.exponential(1.0 / rate_hz), 0, sid))
+            heapq.heappush(events, (t_arr + rng.exponential(1.0 / rate_hz), 0, sid))
         sleep = min((events[0][0] if events else now + 0.001) - time.perf_counter(), 0.0005)
         if sleep > 0:
             time.sleep(sleep)
@@ -231,6 +237,7 @@ def run_load(server: Server, grids, pools, n_sessions: int, rate_hz: float, dura
             server.close_session(sid)
         except N.AmclError:
             pass
+    backlog = len(outstanding)
     lat = np.array(lat)
     st = server.stats()
     return {
@@ -239,6 +246,7 @@ def run_load(server: Server, grids, pools, n_sessions: int, rate_hz: float, dura
         "duration_s": duration_s,
         "requests_measured": int(done_req),
         "submitted": int(submitted),
+        "backlog_at_end": int(backlog),
         "weights_per_s": weights / duration_s,
         "p50_ms": float(np.percentile(lat, 50) * 1e3) if lat.size else None,
         "p99_ms": float(np.percentile(lat, 99) * 1e3) if lat.size else None,
@@ -247,6 +255,64 @@ def run_load(server: Server, grids, pools, n_sessions: int, rate_hz: float, dura
         "admission_waiting": len(admission),
         "dropped_behind": int(dropped),
     }
+
+
+def run_capacity(server: Server, grids, pools, n_sessions: int, duration_s: float, p_range=(1000, 100000),
+                 n_range=(500, 10000), seed=0, depth=2, warmup_s=1.0, odom=None):
+    """The server's capacity on the session mix: every session keeps `depth` requests
+    queued (closed loop, so every step batches every session with work); returns the
+    completed particle x point weights per second."""
+    from . import synth as S
+
+    rng = np.random.default_rng(seed)
+    odom = odom if odom is not None else (*S.ODOM_MODS, 0.05, 0.0, 0.0, 0.01)
+    specs = {}
+    for _ in range(n_sessions):
+        gi = int(rng.integers(len(grids)))
+        pose, scan, rg = pools[gi][int(rng.integers(len(pools[gi])))]
+        P = log_uniform_int(rng, *p_range)
+        n = min(log_uniform_int(rng, *n_range), scan.shape[0])
+        init8 = [pose[0], pose[1], pose[2], pose[3], 0.3, 0.3, 0.05, 0.1]
+        sid = server.open_session(grids[gi], P, seed * 1000 + len(specs) + 1, P, init8)
+        if sid is None:
+            break
+        specs[sid] = (P * n, scan[:n], rg)
+    outstanding = {}
+
+    def submit(sid):
+        w, scan, rg = specs[sid]
+        outstanding[server.submit(sid, scan, rg, odom, 0.5, 0.1, 0.0, 0.0, True)] = (sid, w)
+
+    for sid in specs:
+        for _ in range(depth):
+            submit(sid)
+    t0 = time.perf_counter()
+    t_meas, t_end = t0 + warmup_s, t0 + warmup_s + duration_s
+    weights, done = 0, 0
+    while True:
+        now = time.perf_counter()
+        if now >= t_end:
+            break
+        got = server.poll()
+        for (ticket, sid, status, ts, td, mean) in got:
+            info = outstanding.pop(ticket, None)
+            if info is None:
+                continue
+            if status == 0 and td >= t_meas:
+                weights += info[1]
+                done += 1
+            submit(info[0])
+        if not got:
+            time.sleep(0.0002)
+    deadline = time.perf_counter() + 60.0
+    while outstanding and time.perf_counter() < deadline:  # drain before closing the sessions
+        for (ticket, *_rest) in server.poll():
+            outstanding.pop(ticket, None)
+        time.sleep(0.0005)
+    for sid in specs:
+        server.close_session(sid)
+    return {"sessions": len(specs), "depth": depth, "duration_s": duration_s, "requests": done,
+            "weights_per_s": weights / duration_s}
 
 
 def run_plain(grids, pools, n_requests: int, p_range=(1000, 100000), n_range=(500, 10000), seed=0, odom=None):
@@ -327,7 +393,7 @@ def run_plain_open(grids, pools, n_sessions: int, rate_hz: float, duration_s: fl
             break
         while events and events[0][0] <= now:
             t, sid = heapq.heappop(events)
-            if waiting[sid] >= max_queue:
+            if max_queue is not None and waiting[sid] >= max_queue:
                 dropped += 1
             else:
                 fifo.append((t, sid))
