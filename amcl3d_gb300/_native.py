@@ -109,6 +109,8 @@ _SIGS = {
     "amcl_batch_stage": [_vp, _int, _fp, _u32, _u32, _fp, _u32, _dp, _d, _d, _d, _d, _int],
     "amcl_batch_stage_many": [_vp, _u32, C.POINTER(_int), C.POINTER(_vp), C.POINTER(_u32), _u32, C.POINTER(_vp),
                               C.POINTER(_u32), _dp, _d, _d, _d, _d, _int],
+    "amcl_batch_stage_packed": [_vp, _u32, C.POINTER(_int), _fp, C.POINTER(_u32), _u32, _fp, C.POINTER(_u32), _dp,
+                                _d, _d, _d, _d, _int],
     "amcl_batch_step": [_vp],
     "amcl_batch_wait": [_vp],
     "amcl_batch_get_mean": [_vp, _int, _fp, _dp],

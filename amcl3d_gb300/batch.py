@@ -101,6 +101,33 @@ class FilterBatch:
                N.dptr(od) if od is not None else None, float(alpha), float(sigma), float(roll), float(pitch),
                1 if resample else 0)
 
+    def stage_packed(self, slots, cloud, counts, range_data=None, range_counts=None, odom=None, alpha=0.5,
+                     sigma=0.1, roll=0.0, pitch=0.0, resample=True) -> None:
+        """stage() for many filters from one packed cloud: slots[k] takes the next
+        counts[k] rows of `cloud` ((total, 3 or 4) float32) and the next range_counts[k]
+        rows of range_data ((total, 4)); odom as in stage_many."""
+        count = len(slots)
+        pts, stride = _cloud_array(cloud)
+        sl = np.ascontiguousarray(slots, dtype=np.int32)
+        ns = np.ascontiguousarray(counts, dtype=np.uint32)
+        if ns.shape[0] != count or int(ns.sum()) != pts.shape[0]:
+            raise ValueError("stage_packed: counts must cover the packed cloud, one per slot")
+        rg = nrs = None
+        if range_data is not None:
+            rg = _ranges_array(range_data)
+            nrs = np.ascontiguousarray(range_counts, dtype=np.uint32)
+            if nrs.shape[0] != count or int(nrs.sum()) != rg.shape[0]:
+                raise ValueError("stage_packed: range_counts must cover range_data, one per slot")
+        od = None
+        if odom is not None:
+            o = np.asarray(odom, dtype=np.float64)
+            od = np.ascontiguousarray(np.broadcast_to(o, (count, 8)) if o.ndim == 1 else o.reshape(count, 8))
+        N.call("amcl_batch_stage_packed", self._h, count, sl.ctypes.data_as(C.POINTER(C.c_int)), N.fptr(pts),
+               ns.ctypes.data_as(C.POINTER(C.c_uint32)), stride, N.fptr(rg) if rg is not None and rg.size else None,
+               nrs.ctypes.data_as(C.POINTER(C.c_uint32)) if nrs is not None else None,
+               N.dptr(od) if od is not None else None, float(alpha), float(sigma), float(roll), float(pitch),
+               1 if resample else 0)
+
     def step(self) -> None:
         N.call("amcl_batch_step", self._h)
 

@@ -973,6 +973,14 @@ int pack_steps(amcl_batch_s* b)
   uint32_t ns = 0, nb = 0;
   uint64_t nc = 0, nr = 0;
   b->step_slots.clear();
+  struct Copy
+  {
+    void* dst;
+    const void* src;
+    size_t bytes;
+  };
+  std::vector<Copy> copies;  // into the pinned staging buffers, run together below
+  uint64_t copy_bytes = 0;
   const int threads = b->threads;
   std::vector<const amcl_grid_s*> step_grid;  // grid of each step that gathers
   for (uint32_t si = 0; si < b->slots.size(); ++si)
@@ -997,12 +1005,13 @@ int pack_steps(amcl_batch_s* b)
       return fail(AMCL_ERANGE, "batch: staged clouds exceed max_points_per_step");
     st.c_off = nc;
     if (st.N)
-      std::memcpy(hc + nc, sl.cloud.data(), st.N * sizeof(float4));
+      copies.push_back({ hc + nc, sl.cloud.data(), st.N * sizeof(float4) });
     nc += st.N;
     st.r_off = static_cast<uint32_t>(nr);
     if (st.nr)
-      std::memcpy(hr + nr, sl.ranges.data(), st.nr * sizeof(float4));
+      copies.push_back({ hr + nr, sl.ranges.data(), st.nr * sizeof(float4) });
     nr += st.nr;
+    copy_bytes += (st.N + st.nr) * sizeof(float4);
     st.flags = ST_UPDATE | (sl.predict ? ST_PREDICT : 0u) | (sl.resample ? ST_RESAMPLE : 0u);
     st.cloud_sum = static_cast<uint32_t>(sl.cloud_sum);
     const float rollf = static_cast<float>(sl.roll), pitchf = static_cast<float>(sl.pitch);
@@ -1058,6 +1067,8 @@ int pack_steps(amcl_batch_s* b)
     b->step_slots.push_back(si);
     sl.staged = false;
   }
+  host_parallel_for(static_cast<uint32_t>(copies.size()), copy_threads(copy_bytes),
+                    [&](uint32_t i) { std::memcpy(copies[i].dst, copies[i].src, copies[i].bytes); });
   assign_grid_slots(b, hs, step_grid);
   b->n_steps = ns;
   b->n_blk = nb;
@@ -1529,6 +1540,64 @@ extern "C" int amcl_batch_stage_many(amcl_batch_t b, uint32_t count, const int* 
                                 nrk, odom8 ? odom8 + 8ull * k : nullptr, alpha, sigma, roll, pitch, resample);
     if (rc)
       return rc;
+  }
+  return AMCL_OK;
+}
+
+extern "C" int amcl_batch_stage_packed(amcl_batch_t b, uint32_t count, const int* slots, const float* xyz,
+                                       const uint32_t* n, uint32_t stride_floats, const float* ranges4,
+                                       const uint32_t* nr, const double* odom8, double alpha, double sigma,
+                                       double roll, double pitch, int resample)
+{
+  if (!b || (count && (!slots || !n)) || stride_floats < 3)
+    return fail(AMCL_EINVAL, "amcl_batch_stage_packed: bad arguments");
+  std::lock_guard<std::mutex> lock(b->mu);
+  // offsets into the packed arrays, and every check before anything is copied
+  std::vector<uint64_t> c_off(count), r_off(count);
+  uint64_t pts = 0, rgs = 0;
+  std::vector<uint8_t> seen(b->slots.size(), 0);
+  for (uint32_t k = 0; k < count; ++k)
+  {
+    c_off[k] = pts;
+    r_off[k] = rgs;
+    pts += n[k];
+    rgs += nr ? nr[k] : 0;
+    int rc = slot_check(b, slots[k]);
+    if (rc)
+      return rc;
+    if (!b->slots[slots[k]].initialized)
+      return fail(AMCL_ESTATE, "amcl_batch_stage_packed: filter not initialised");
+    if (seen[slots[k]]++)
+      return fail(AMCL_EINVAL, "amcl_batch_stage_packed: a slot appears twice");
+    if (nr && nr[k] > MAX_RANGES)
+      return fail(AMCL_ERANGE, "amcl_batch_stage_packed: more than 64 range measurements");
+  }
+  if ((pts && !xyz) || (rgs && !ranges4))
+    return fail(AMCL_EINVAL, "amcl_batch_stage_packed: null cloud or ranges");
+  for (uint32_t k = 0; k < count; ++k)  // sizes first (allocation stays on this thread)
+  {
+    BatchSlot& sl = b->slots[slots[k]];
+    sl.cloud.resize(n[k]);
+    sl.ranges.resize(nr ? nr[k] : 0);
+  }
+  host_parallel_for(count, copy_threads((pts + rgs) * 16), [&](uint32_t k) {
+    BatchSlot& sl = b->slots[slots[k]];
+    pack_cloud(xyz + c_off[k] * stride_floats, n[k], stride_floats, sl.cloud.data());
+    if (!sl.ranges.empty())
+      std::memcpy(sl.ranges.data(), ranges4 + 4 * r_off[k], sl.ranges.size() * 16);
+  });
+  for (uint32_t k = 0; k < count; ++k)
+  {
+    BatchSlot& sl = b->slots[slots[k]];
+    sl.predict = odom8 != nullptr;
+    if (odom8)
+      std::memcpy(sl.odom, odom8 + 8ull * k, sizeof(sl.odom));
+    sl.alpha = alpha;
+    sl.sigma = sigma;
+    sl.roll = roll;
+    sl.pitch = pitch;
+    sl.resample = resample != 0;
+    sl.staged = true;
   }
   return AMCL_OK;
 }

@@ -6,7 +6,9 @@
 #include <cuda_fp16.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <atomic>
+#include <thread>
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -224,6 +226,41 @@ struct ProfScope
 };
 
 inline unsigned ceil_div(uint64_t a, uint64_t b) { return static_cast<unsigned>((a + b - 1) / b); }
+
+// Runs f(i) for i in [0, n) on up to `threads` host threads (the caller's included),
+// items taken in order from a shared counter; serial for threads <= 1.
+template <typename F>
+void host_parallel_for(uint32_t n, unsigned threads, F f)
+{
+  threads = std::min<unsigned>(threads, n);
+  if (threads <= 1)
+  {
+    for (uint32_t i = 0; i < n; ++i)
+      f(i);
+    return;
+  }
+  std::atomic<uint32_t> next{ 0 };
+  auto work = [&] {
+    for (uint32_t i = next.fetch_add(1); i < n; i = next.fetch_add(1))
+      f(i);
+  };
+  std::vector<std::thread> pool;
+  for (unsigned t = 1; t < threads; ++t)
+    pool.emplace_back(work);
+  work();
+  for (auto& th : pool)
+    th.join();
+}
+
+// Host threads for copies of `bytes` in total: one below 1 MB, else up to 8 (or half
+// the hardware threads).
+inline unsigned copy_threads(uint64_t bytes)
+{
+  if (bytes < (1u << 20))
+    return 1;
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency() / 2);
+  return std::min(8u, hw);
+}
 
 // Runs `set` (returning an AMCL status) once for the current device and remembers
 // success per device ordinal (0-63) in `done`: kernel attributes are per device.

@@ -299,6 +299,14 @@ int amcl_batch_get_particles(amcl_batch_t b, int slot, float* p7, uint32_t cap);
 int amcl_batch_stage(amcl_batch_t b, int slot, const float* xyz, uint32_t n, uint32_t stride_floats,
                      const float* ranges4, uint32_t nr, const double* odom8, double alpha, double sigma, double roll,
                      double pitch, int resample);
+/* amcl_batch_stage for `count` filters whose clouds are packed one after another in
+ * one host array: filter k (slot slots[k], each slot at most once) takes the next n[k]
+ * points of xyz (stride_floats apart) and the next nr[k] ranges of ranges4 (nr NULL:
+ * none), odometry odom8[8k..8k+7] (NULL: no predict).  Every argument is checked
+ * before anything is staged; the copies run on several host threads when large. */
+int amcl_batch_stage_packed(amcl_batch_t b, uint32_t count, const int* slots, const float* xyz, const uint32_t* n,
+                            uint32_t stride_floats, const float* ranges4, const uint32_t* nr, const double* odom8,
+                            double alpha, double sigma, double roll, double pitch, int resample);
 /* amcl_batch_stage for `count` filters in one call: slots[k] gets clouds[k] (n[k]
  * points, stride_floats apart), nr[k] ranges at ranges4[k] (nr and ranges4 may be
  * NULL: no ranges), odometry odom8[8k..8k+7] (odom8 NULL: no predict); the other

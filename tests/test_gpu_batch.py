@@ -214,3 +214,52 @@ def test_batch_more_grids_than_slots(amcl):
         for i, (sl, sp) in enumerate(zip(slots, specs)):
             np.testing.assert_array_equal(B.particles(sl, sp["P"]), alone[i][s], err_msg=f"filter {i} step {s}")
     B.close()
+
+
+def test_stage_packed_equals_stage_many(amcl, world):
+    """Filters staged from one packed cloud (amcl_batch_stage_packed, copied on host
+    threads) step exactly as the same filters staged one array each."""
+    from amcl3d_gb300.batch import FilterBatch
+
+    grids, specs = world
+    sps = [sp for sp in specs if sp["roll"] == 0.0]
+    odom = (*MODS, 0.05, 0.01, 0.0, 0.02)
+    out = []
+    for packed in (False, True):
+        B = FilterBatch(max_filters=len(sps), max_particles=sum(sp["P"] + 256 for sp in sps),
+                        max_points_per_step=8000)
+        slots = [B.add(grids[sp["grid"]], sp["P"], sp["seed"]) for sp in sps]
+        for sl, sp in zip(slots, sps):
+            B.set_particles(sl, sp["parts"])
+        res = []
+        for s in range(2):
+            clouds = [sp["scans"][s] for sp in sps]
+            rgs = [sp["ranges"] for sp in sps]
+            if packed:
+                B.stage_packed(slots, np.concatenate(clouds), [c.shape[0] for c in clouds], np.concatenate(rgs),
+                               [r.shape[0] for r in rgs], odom)
+            else:
+                B.stage_many(slots, clouds, rgs, odom)
+            B.step()
+            B.wait()
+            res.append([B.particles(sl, sp["P"]) for sl, sp in zip(slots, sps)])
+        out.append(res)
+        B.close()
+    for a, b in zip(out[0], out[1]):
+        for x, y in zip(a, b):
+            np.testing.assert_array_equal(x, y)
+
+
+def test_stage_packed_rejects_a_repeated_slot(amcl, world):
+    from amcl3d_gb300 import _native as N
+    from amcl3d_gb300.batch import FilterBatch
+
+    grids, specs = world
+    sp = specs[1]
+    B = FilterBatch(max_filters=2, max_particles=2 * (sp["P"] + 256), max_points_per_step=4000)
+    sl = B.add(grids[sp["grid"]], sp["P"], 1)
+    B.set_particles(sl, sp["parts"])
+    cloud = sp["scans"][0]
+    with pytest.raises(N.AmclError):
+        B.stage_packed([sl, sl], np.concatenate([cloud, cloud]), [cloud.shape[0]] * 2)
+    B.close()
