@@ -15,11 +15,13 @@
 // together (each lane's arena can hold the whole budget, so a session fits in any
 // lane); beyond it amcl_server_open_session fails with AMCL_ENOMEM and the caller
 // retries once sessions close.
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -63,11 +65,15 @@ struct amcl_server_s
     amcl_batch_t batch = nullptr;
     std::thread worker;
     uint32_t sessions = 0;
+    uint64_t particles = 0;       // particle capacity of the lane's sessions (its share of the load)
+    std::vector<int64_t> ids;     // the lane's sessions
+    uint64_t pending = 0;         // requests queued on the lane's sessions
+    // signalled when one of them gets a request (held by pointer: lanes live in a vector)
+    std::unique_ptr<std::condition_variable> cv = std::make_unique<std::condition_variable>();
   };
   std::vector<Lane> lanes;
   uint64_t budget = 0, admitted = 0;  // particle capacity of the open sessions
   std::mutex mu;
-  std::condition_variable cv;
   std::map<int64_t, Session> sessions;
   int64_t next_session = 1;
   uint64_t next_ticket = 1;
@@ -94,50 +100,70 @@ void worker_loop(amcl_server_s* S, int lane)
     uint64_t weights;
   };
   std::vector<InFlight> flight, next;
+  struct Taken
+  {
+    int64_t session;
+    int slot;
+    Request r;
+  };
+  std::vector<Taken> taken;
+  std::vector<amcl_server_result> failed;
+  amcl_server_s::Lane& L = S->lanes[lane];
   double t_launch = 0;
   while (true)
   {
-    // Stage the next step from the pending requests (one per session).
+    // Take the next step's requests (the oldest of each of the lane's sessions) under
+    // the server lock, then stage them (copying the clouds) without it, so submits
+    // and the other lanes are not held up by the copies.
     next.clear();
+    taken.clear();
+    failed.clear();
     {
       std::unique_lock<std::mutex> lock(S->mu);
       if (flight.empty())
-        S->cv.wait(lock, [&] {
-          if (S->stop)
-            return true;
-          for (auto& kv : S->sessions)
-            if (kv.second.lane == lane && !kv.second.pending.empty())
-              return true;
-          return false;
-        });
+        L.cv->wait(lock, [&] { return S->stop || L.pending > 0; });
       if (S->stop && flight.empty())
         return;
-      for (auto& kv : S->sessions)
+      for (int64_t id : L.ids)
       {
-        Session& ss = kv.second;
-        if (ss.lane != lane || ss.pending.empty())
+        auto it = S->sessions.find(id);
+        if (it == S->sessions.end() || it->second.pending.empty())
           continue;
-        Request& r = ss.pending.front();
-        const int rc = amcl_batch_stage(batch, ss.slot, r.n ? r.xyz.data() : nullptr, r.n, 4,
-                                        r.nr ? r.ranges.data() : nullptr, r.nr, r.has_odom ? r.odom : nullptr,
-                                        r.alpha, r.sigma, r.roll, r.pitch, r.resample);
-        InFlight f{ kv.first, ss.slot, r.ticket, r.t_submit, 0 };
-        if (rc != AMCL_OK)
-        {
-          amcl_server_result res{};
-          res.ticket = r.ticket;
-          res.session = kv.first;
-          res.status = rc;
-          res.t_submit = r.t_submit;
-          res.t_done = now_s();
-          S->done.push_back(res);
-          ss.pending.pop_front();
-          continue;
-        }
-        f.weights = 0;
-        next.push_back(f);
+        Session& ss = it->second;
+        taken.push_back(Taken{ id, ss.slot, std::move(ss.pending.front()) });
         ss.pending.pop_front();
         ss.in_flight += 1;
+        L.pending -= 1;
+      }
+    }
+    for (Taken& t : taken)
+    {
+      const Request& r = t.r;
+      const int rc = amcl_batch_stage(batch, t.slot, r.n ? r.xyz.data() : nullptr, r.n, 4,
+                                      r.nr ? r.ranges.data() : nullptr, r.nr, r.has_odom ? r.odom : nullptr,
+                                      r.alpha, r.sigma, r.roll, r.pitch, r.resample);
+      if (rc != AMCL_OK)
+      {
+        amcl_server_result res{};
+        res.ticket = r.ticket;
+        res.session = t.session;
+        res.status = rc;
+        res.t_submit = r.t_submit;
+        res.t_done = now_s();
+        failed.push_back(res);
+        continue;
+      }
+      next.push_back(InFlight{ t.session, t.slot, r.ticket, r.t_submit, 0 });
+    }
+    if (!failed.empty())
+    {
+      std::lock_guard<std::mutex> lock(S->mu);
+      for (auto& res : failed)
+      {
+        S->done.push_back(res);
+        auto it = S->sessions.find(res.session);
+        if (it != S->sessions.end())
+          it->second.in_flight -= 1;
       }
     }
     // Wait for the step in flight, read its results, then launch the next one.
@@ -245,7 +271,8 @@ extern "C" int amcl_server_destroy(amcl_server_t S)
     for (auto& kv : S->sessions)
       kv.second.pending.clear();
   }
-  S->cv.notify_all();
+  for (auto& L : S->lanes)
+    L.cv->notify_all();
   for (auto& L : S->lanes)
     if (L.worker.joinable())
       L.worker.join();
@@ -266,11 +293,13 @@ extern "C" int amcl_server_open_session(amcl_server_t S, amcl_grid_t grid, uint3
     std::lock_guard<std::mutex> lock(S->mu);
     if (S->admitted + need > S->budget)
       return amcl::fail(AMCL_ENOMEM, "amcl_server_open_session: the particle budget is taken (admission refused)");
+    // the lane carrying the fewest particles: requests scale with them
     for (int k = 1; k < static_cast<int>(S->lanes.size()); ++k)
-      if (S->lanes[k].sessions < S->lanes[lane].sessions)
+      if (S->lanes[k].particles < S->lanes[lane].particles)
         lane = k;
     S->admitted += need;  // reserved while the slot is set up (without the server lock)
     S->lanes[lane].sessions += 1;
+    S->lanes[lane].particles += need;
   }
   amcl_batch_t batch = S->lanes[lane].batch;
   int slot = -1;
@@ -287,6 +316,7 @@ extern "C" int amcl_server_open_session(amcl_server_t S, amcl_grid_t grid, uint3
   {
     S->admitted -= need;
     S->lanes[lane].sessions -= 1;
+    S->lanes[lane].particles -= need;
     return rc;
   }
   const int64_t id = S->next_session++;
@@ -294,6 +324,7 @@ extern "C" int amcl_server_open_session(amcl_server_t S, amcl_grid_t grid, uint3
   ss.lane = lane;
   ss.slot = slot;
   ss.capacity = need;
+  S->lanes[lane].ids.push_back(id);
   *session = id;
   return AMCL_OK;
 }
@@ -317,6 +348,8 @@ extern "C" int amcl_server_close_session(amcl_server_t S, int64_t session)
       {
         ss = it->second;
         S->sessions.erase(it);
+        auto& ids = S->lanes[ss.lane].ids;
+        ids.erase(std::remove(ids.begin(), ids.end(), session), ids.end());
         break;
       }
     }
@@ -328,6 +361,7 @@ extern "C" int amcl_server_close_session(amcl_server_t S, int64_t session)
   std::lock_guard<std::mutex> lock(S->mu);
   S->admitted -= ss.capacity;
   S->lanes[ss.lane].sessions -= 1;
+  S->lanes[ss.lane].particles -= ss.capacity;
   return rc;
 }
 
@@ -359,6 +393,7 @@ extern "C" int amcl_server_submit(amcl_server_t S, int64_t session, const float*
   r.roll = roll;
   r.pitch = pitch;
   r.resample = resample;
+  int lane = 0;
   {
     std::lock_guard<std::mutex> lock(S->mu);
     auto it = S->sessions.find(session);
@@ -367,9 +402,11 @@ extern "C" int amcl_server_submit(amcl_server_t S, int64_t session, const float*
     r.ticket = S->next_ticket++;
     if (ticket)
       *ticket = r.ticket;
+    lane = it->second.lane;
     it->second.pending.push_back(std::move(r));
+    S->lanes[lane].pending += 1;
   }
-  S->cv.notify_all();  // the session's lane picks it up
+  S->lanes[lane].cv->notify_one();  // the session's lane picks it up
   return AMCL_OK;
 }
 

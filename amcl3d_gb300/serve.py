@@ -82,6 +82,28 @@ class Server:
                float(sigma), float(roll), float(pitch), 1 if resample else 0, C.byref(t))
         return t.value
 
+    def prepare(self, sid: int, cloud, range_data, odom=None, alpha=0.5, sigma=0.1, roll=0.0, pitch=0.0,
+                resample=True) -> tuple:
+        """The arguments of submit() converted once, for a caller that sends the same
+        request shape again and again (submit_prepared).  The arrays are kept alive by
+        the returned tuple."""
+        pts, stride = _cloud_array(cloud)
+        rg = _ranges_array(range_data)
+        od = None if odom is None else np.ascontiguousarray(odom, dtype=np.float64)
+        keep = (pts, rg, od)
+        args = (self._h, C.c_int64(int(sid)), pts.ctypes.data_as(N._fp), C.c_uint32(pts.shape[0]),
+                C.c_uint32(stride), rg.ctypes.data_as(N._fp) if rg.size else None, C.c_uint32(rg.shape[0]),
+                od.ctypes.data_as(N._dp) if od is not None else None, C.c_double(alpha), C.c_double(sigma),
+                C.c_double(roll), C.c_double(pitch), C.c_int(1 if resample else 0))
+        return keep, args, C.c_uint64()
+
+    def submit_prepared(self, prepared) -> int:
+        _keep, args, t = prepared
+        rc = N.lib.amcl_server_submit(*args, C.byref(t))
+        if rc != 0:
+            raise N.AmclError(rc, "amcl_server_submit", N.lib.amcl_last_error().decode())
+        return t.value
+
     def poll(self) -> list:
         out = []
         while True:
@@ -164,7 +186,7 @@ def run_load(server: Server, grids, pools, n_sessions: int, rate_hz: float, dura
         sid = server.open_session(grids[spec.grid], spec.P, spec.seed, spec.P, init8)
         if sid is None:
             return False
-        specs[sid] = (spec, scan, rg)
+        specs[sid] = (spec, scan, rg, server.prepare(sid, scan, rg, odom, 0.5, 0.1, 0.0, 0.0, True))
         return True
 
     for _ in range(n_sessions):
@@ -179,6 +201,7 @@ def run_load(server: Server, grids, pools, n_sessions: int, rate_hz: float, dura
     outstanding = {}
     per_session = {}
     lat = []
+    lat_srv = []  # from the submit call to the result (the server alone)
     weights = 0
     done_req = 0
     t_end = t0 + warmup_s + duration_s
@@ -198,6 +221,7 @@ def run_load(server: Server, grids, pools, n_sessions: int, rate_hz: float, dura
             per_session[sid] = per_session.get(sid, 1) - 1
             if td >= t_meas and status == 0:
                 lat.append(td - info[1])
+                lat_srv.append(td - ts)
                 weights += info[0]
                 done_req += 1
         # churn: one session leaves, a new one arrives (waiting for admission)
@@ -220,11 +244,11 @@ def run_load(server: Server, grids, pools, n_sessions: int, rate_hz: float, dura
             t_arr, _, sid = heapq.heappop(events)
             if sid not in specs:
                 continue
-            spec, scan, rg = specs[sid]
+            spec, scan, rg, prepared = specs[sid]
             if max_queue is not None and per_session.get(sid, 0) >= max_queue:
                 dropped += 1  # the session is that far behind: skip this scan, as the node's threshold gating does
             else:
-                ticket = server.submit(sid, scan, rg, odom, 0.5, 0.1, 0.0, 0.0, True)
+                ticket = server.submit_prepared(prepared)
                 outstanding[ticket] = (spec.P * scan.shape[0], t_arr)
                 per_session[sid] = per_session.get(sid, 0) + 1
                 submitted += 1
@@ -239,6 +263,7 @@ def run_load(server: Server, grids, pools, n_sessions: int, rate_hz: float, dura
             pass
     backlog = len(outstanding)
     lat = np.array(lat)
+    lat_srv = np.array(lat_srv)
     st = server.stats()
     return {
         "sessions": n_sessions,
@@ -250,6 +275,8 @@ def run_load(server: Server, grids, pools, n_sessions: int, rate_hz: float, dura
         "weights_per_s": weights / duration_s,
         "p50_ms": float(np.percentile(lat, 50) * 1e3) if lat.size else None,
         "p99_ms": float(np.percentile(lat, 99) * 1e3) if lat.size else None,
+        "server_p50_ms": float(np.percentile(lat_srv, 50) * 1e3) if lat_srv.size else None,
+        "server_p99_ms": float(np.percentile(lat_srv, 99) * 1e3) if lat_srv.size else None,
         "mean_batch": st["requests"] / max(st["steps"], 1),
         "max_batch": st["max_batch"],
         "admission_waiting": len(admission),
@@ -276,12 +303,12 @@ def run_capacity(server: Server, grids, pools, n_sessions: int, duration_s: floa
         sid = server.open_session(grids[gi], P, seed * 1000 + len(specs) + 1, P, init8)
         if sid is None:
             break
-        specs[sid] = (P * n, scan[:n], rg)
+        specs[sid] = (P * n, server.prepare(sid, scan[:n], rg, odom, 0.5, 0.1, 0.0, 0.0, True))
     outstanding = {}
 
     def submit(sid):
-        w, scan, rg = specs[sid]
-        outstanding[server.submit(sid, scan, rg, odom, 0.5, 0.1, 0.0, 0.0, True)] = (sid, w)
+        w, prepared = specs[sid]
+        outstanding[server.submit_prepared(prepared)] = (sid, w)
 
     for sid in specs:
         for _ in range(depth):

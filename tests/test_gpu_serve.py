@@ -2,7 +2,7 @@
 same filter stepped alone (whatever else is in flight, on one lane or spread over
 concurrent lanes), admission refuses sessions
 beyond the budget, and host-side failures (unknown session, a session that leaves
-mid-stream, NaN inputs) stay contained."""
+mid-stream, with requests still queued or running, NaN inputs) stay contained."""
 
 import time
 
@@ -118,4 +118,47 @@ def test_admission_and_host_failures(amcl, scene):
     assert s3 is not None
     t3 = srv.submit(s3, sp["scans"][1], sp["ranges"], ODOM)
     assert drain(srv, 1)[0][0] == t3
+    srv.close()
+
+
+@pytest.mark.parametrize("lanes", [1, 4])
+def test_close_with_requests_queued(amcl, scene, lanes):
+    """A session closed while its requests are still queued or on the GPU: the close
+    waits for them (they complete, results delivered), frees the slot, and the other
+    sessions' results are still exactly those of the same filters stepped alone."""
+    from amcl3d_gb300.serve import Server
+
+    G, sessions = scene
+    nreq = 3
+    srv = Server(max_sessions=8, max_particles=40000, max_points_per_step=10000, lanes=lanes)
+    sids = []
+    for sp in sessions:
+        x, y, z, a = sp["pose"]
+        sids.append(srv.open_session(G, sp["P"], sp["seed"], sp["P"], [x, y, z, a, 0.3, 0.3, 0.05, 0.1]))
+    leaving = sids[2]  # the 12,000-particle session: its steps take longest
+    tickets = {}
+    for r in range(nreq):
+        for sid, sp in zip(sids, sessions):
+            tickets[srv.submit(sid, sp["scans"][r], sp["ranges"], ODOM)] = (sid, r)
+    srv.close_session(leaving)  # returns once its queued and running requests are done
+    got = drain(srv, len(tickets))
+    assert len(got) == len(tickets)
+    per = {sid: {} for sid in sids}
+    for ticket, sid, status, ts, td, mean in got:
+        assert status == 0
+        per[sid][tickets[ticket][1]] = np.array(mean, np.float32)
+    assert len(per[leaving]) == nreq
+    for sid, sp in zip(sids, sessions):
+        want = alone_means(amcl, G, sp, nreq)
+        for r in range(nreq):
+            np.testing.assert_array_equal(per[sid][r], want[r], err_msg=f"session {sid} request {r}")
+    from amcl3d_gb300 import _native as N
+
+    with pytest.raises(N.AmclError):
+        srv.submit(leaving, sessions[2]["scans"][0], sessions[2]["ranges"], ODOM)  # gone
+    x, y, z, a = sessions[2]["pose"]
+    assert srv.open_session(G, 12000, 9, 12000, [x, y, z, a, 0.3, 0.3, 0.05, 0.1]) is not None  # slot reused
+    for sid in sids:
+        if sid != leaving:
+            srv.close_session(sid)
     srv.close()
