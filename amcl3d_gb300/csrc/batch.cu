@@ -520,9 +520,40 @@ struct BatchSlot
   bool stats_valid = false;
 };
 
+// Side streams and events that let a step's weighting launches (one per fused queue)
+// run as parallel branches: forked from the batch stream, joined back before blend.
+constexpr int N_SIDE = 5;
+struct Branches
+{
+  cudaStream_t side[N_SIDE] = {};
+  cudaEvent_t fork = nullptr;
+  cudaEvent_t join[64] = {};
+  int init()
+  {
+    for (auto& s : side)
+      AMCL_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    AMCL_CUDA_TRY(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    for (auto& e : join)
+      AMCL_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    return AMCL_OK;
+  }
+  ~Branches()
+  {
+    for (auto s : side)
+      if (s)
+        cudaStreamDestroy(s);
+    if (fork)
+      cudaEventDestroy(fork);
+    for (auto e : join)
+      if (e)
+        cudaEventDestroy(e);
+  }
+};
+
 struct amcl_batch_s
 {
   StreamHolder st;
+  Branches br;
   uint32_t max_filters = 0;
   uint64_t max_particles = 0, max_points = 0;
   std::vector<BatchSlot> slots;
@@ -619,8 +650,48 @@ size_t split_smem(const amcl_batch_s* b)
 
 // Persistent launches of one (storage, sum) class: one per fused queue in `mask`, sized
 // to the blocks that fit on every SM at once.
+// Hands out the stream of each fused-queue launch of a step: the batch stream when
+// there is one launch, else a side stream forked from it (joined by join()), so the
+// queues' persistent kernels (one per grid slot) run side by side and their tails overlap.
+struct Fork
+{
+  amcl_batch_s* b;
+  cudaStream_t main;
+  int launches;
+  int used = 0;
+  int next(cudaStream_t* out)
+  {
+    if (launches <= 1)
+    {
+      *out = main;
+      return AMCL_OK;
+    }
+    if (used == 0)
+      AMCL_CUDA_TRY(cudaEventRecord(b->br.fork, main));
+    if (used >= 64)
+      return fail(AMCL_ERANGE, "batch: more than 64 weighting launches in one step");
+    *out = b->br.side[used % N_SIDE];
+    AMCL_CUDA_TRY(cudaStreamWaitEvent(*out, b->br.fork, 0));
+    return AMCL_OK;
+  }
+  int done(cudaStream_t s)  // after the launch on s
+  {
+    if (launches <= 1)
+      return AMCL_OK;
+    AMCL_CUDA_TRY(cudaEventRecord(b->br.join[used], s));
+    ++used;
+    return AMCL_OK;
+  }
+  int join()
+  {
+    for (int i = 0; i < used; ++i)
+      AMCL_CUDA_TRY(cudaStreamWaitEvent(main, b->br.join[i], 0));
+    return AMCL_OK;
+  }
+};
+
 template <int STORAGE, int SUM, int MAXT>
-int launch_fused_class(amcl_batch_s* b, const BatchDev& d, int threads, uint32_t chunk, size_t smem, cudaStream_t s,
+int launch_fused_class(amcl_batch_s* b, const BatchDev& d, int threads, uint32_t chunk, size_t smem, Fork& fk,
                        uint64_t mask)
 {
   const int cls = weight_class(STORAGE, SUM);
@@ -629,6 +700,10 @@ int launch_fused_class(amcl_batch_s* b, const BatchDev& d, int threads, uint32_t
     const int q = fused_queue(cls, slot < BATCH_GRIDS ? slot : -1);
     if (!(mask >> q & 1u))
       continue;
+    cudaStream_t s = nullptr;
+    int rc = fk.next(&s);
+    if (rc)
+      return rc;
     int per_sm = 0;
     if (slot < BATCH_GRIDS)
     {
@@ -651,6 +726,8 @@ int launch_fused_class(amcl_batch_s* b, const BatchDev& d, int threads, uint32_t
                                                                          chunk);
     }
     AMCL_LAUNCH_CHECK("k_b_weight");
+    if ((rc = fk.done(s)))
+      return rc;
   }
   return AMCL_OK;
 }
@@ -659,15 +736,16 @@ template <int MAXT>
 int launch_fused_classes(amcl_batch_s* b, const BatchDev& d, int threads, uint32_t chunk, size_t smem, cudaStream_t s,
                          uint64_t mask)
 {
+  Fork fk{ b, s, __builtin_popcountll(mask & ((1ull << N_FUSED_Q) - 1)) };
   int rc;
-  if ((rc = launch_fused_class<AMCL_GRID_F32, 0, MAXT>(b, d, threads, chunk, smem, s, mask)) ||
-      (rc = launch_fused_class<AMCL_GRID_F32, 1, MAXT>(b, d, threads, chunk, smem, s, mask)) ||
-      (rc = launch_fused_class<AMCL_GRID_F16, 0, MAXT>(b, d, threads, chunk, smem, s, mask)) ||
-      (rc = launch_fused_class<AMCL_GRID_F16, 1, MAXT>(b, d, threads, chunk, smem, s, mask)) ||
-      (rc = launch_fused_class<AMCL_GRID_U8, 0, MAXT>(b, d, threads, chunk, smem, s, mask)) ||
-      (rc = launch_fused_class<AMCL_GRID_U8, 1, MAXT>(b, d, threads, chunk, smem, s, mask)))
+  if ((rc = launch_fused_class<AMCL_GRID_F32, 0, MAXT>(b, d, threads, chunk, smem, fk, mask)) ||
+      (rc = launch_fused_class<AMCL_GRID_F32, 1, MAXT>(b, d, threads, chunk, smem, fk, mask)) ||
+      (rc = launch_fused_class<AMCL_GRID_F16, 0, MAXT>(b, d, threads, chunk, smem, fk, mask)) ||
+      (rc = launch_fused_class<AMCL_GRID_F16, 1, MAXT>(b, d, threads, chunk, smem, fk, mask)) ||
+      (rc = launch_fused_class<AMCL_GRID_U8, 0, MAXT>(b, d, threads, chunk, smem, fk, mask)) ||
+      (rc = launch_fused_class<AMCL_GRID_U8, 1, MAXT>(b, d, threads, chunk, smem, fk, mask)))
     return rc;
-  return AMCL_OK;
+  return fk.join();
 }
 
 // The weighting of a packed step: the fused queues in `mask` (bits 0 .. N_FUSED_Q-1),
@@ -1245,6 +1323,8 @@ extern "C" int amcl_batch_create(amcl_batch_t* out, uint32_t max_filters, uint64
     return fail(AMCL_EINVAL, "amcl_batch_create: bad arguments");
   amcl_batch_s* b = new amcl_batch_s();
   int rc = b->st.init(stream);
+  if (!rc)
+    rc = b->br.init();
   const uint64_t cap = align256(max_particles) + 256ull * max_filters;  // per-slot alignment slack
   const uint64_t pts = std::max<uint64_t>(max_points_per_step, 1);
   const uint64_t rng = 64ull * max_filters;

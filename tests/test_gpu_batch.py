@@ -263,3 +263,39 @@ def test_stage_packed_rejects_a_repeated_slot(amcl, world):
     with pytest.raises(N.AmclError):
         B.stage_packed([sl, sl], np.concatenate([cloud, cloud]), [cloud.shape[0]] * 2)
     B.close()
+
+
+def test_auto_mode_wide_and_long_filters(amcl, world):
+    """The automatic weighting choice on a step holding a wide filter with a short scan
+    and a narrow one with a long scan, on two maps' worth of launches: both equal the
+    same filters stepped alone."""
+    from amcl3d_gb300.batch import FilterBatch
+
+    grids, specs = world
+    m_wide = S.make_map(31, size_m=(8.0, 6.0, 3.0), n_boxes=8)
+    pose = S.free_pose(m_wide, 81, height=1.2, clearance=0.4)
+    wide = dict(grid=0, P=100000, scans=[S.ray_cast(m_wide, pose, n_max=150, max_range=8.0, seed=82 + s)
+                                          for s in range(2)],
+                parts=S.particles_around(pose, 100000, 83), ranges=S.beacons(m_wide, pose, 3, seed=84), roll=0.0,
+                pitch=0.0, seed=2001)
+    long_scan = dict(specs[3])  # on the other map: two fused launches, run as parallel branches
+    long_scan["P"] = 2000
+    long_scan["parts"] = specs[3]["parts"][:2000]
+    mix = [wide, long_scan]
+    steps = 2
+    alone = [run_alone(amcl, grids, sp, steps) for sp in mix]
+    B = FilterBatch(max_filters=4, max_particles=110000, max_points_per_step=4000)
+    B.set_split(0)
+    slots = []
+    for sp in mix:
+        sl = B.add(grids[sp["grid"]], sp["P"], sp["seed"])
+        B.set_particles(sl, sp["parts"])
+        slots.append(sl)
+    odom = (*MODS, 0.05, 0.01, 0.0, 0.02)
+    for s in range(steps):
+        for sl, sp in zip(slots, mix):
+            B.stage(sl, sp["scans"][s], sp["ranges"], odom, 0.5, 0.1)
+        B.step()
+        B.wait()
+        for i, (sl, sp) in enumerate(zip(slots, mix)):
+            np.testing.assert_array_equal(B.particles(sl, sp["P"]), alone[i][s][0], err_msg=f"filter {i} step {s}")
