@@ -680,6 +680,7 @@ def storage_section(ft, seed, g_host, steps=5, sample=64):
     and at every step the per-particle weights of a particle sample against the FP64
     oracle (the mean in double of the FP64 probabilities of the cells the reference's
     arithmetic selects)."""
+    import amcl3d_gb300 as A
     import oracle as O
     from amcl3d_gb300 import synth as S
 
@@ -700,18 +701,28 @@ def storage_section(ft, seed, g_host, steps=5, sample=64):
             pf.resample()
         pf.profile(True)
         pf.profile_read(reset=True)
-        weights, errs = 0, []
+        weights, errs, errs_c = 0, [], []
         for k in range(steps):
             i = (2 + k) % N_SCANS
             pf.predict(*S.ODOM_MODS, *odos[i])
             if p64 is not None:
-                # the sample: particles of this step's (predicted) set, weighed by computeCloudWeight
-                pose4 = pf.particles()[rng.choice(P, sample, replace=False), :4]
+                # the sample: particles of this step's (predicted) set; their weights with the
+                # reference's float running sum (computeCloudWeight) and with the compensated sum
+                samp = pf.particles()[rng.choice(P, sample, replace=False)]
+                pose4 = samp[:, :4]
                 _, cells = O.cloud_weights(g_host, pose4, scans[i], 0.0, 0.0, yaw_trig=1, cells=True)
                 exact = np.array([p64[c[c >= 0]].mean() if (c >= 0).sum() > 10 else 0.0 for c in cells])
                 got = G.computeCloudWeights(pose4, scans[i]).astype(np.float64)
                 mask = exact > 0
                 errs.append(np.abs(got[mask] - exact[mask]) / exact[mask])
+                side = A.ParticleFilter(seed=1)
+                side.set_option(1, 1)
+                side.set_particles(samp)
+                side.update(G, scans[i], np.zeros((0, 4), np.float32), 1.0, 0.1, 0.0, 0.0)
+                gotc = side.particles()[:, 5].astype(np.float64)  # normalised by the sample's exact sum
+                want = exact / exact.sum()
+                errs_c.append(np.abs(gotc[mask] - want[mask]) / want[mask])
+                del side
             pf.update(G, scans[i], ranges[i], 0.5, 0.1, 0.0, 0.0)
             pf.getMean()
             pf.resample()
@@ -721,12 +732,19 @@ def storage_section(ft, seed, g_host, steps=5, sample=64):
         ms, n = prof["cloud_weight"]
         bpc = {"f32": 4, "f16": 2, "u8": 1}[storage]
         e = np.concatenate(errs) if errs else np.zeros(0)
+        ec = np.concatenate(errs_c) if errs_c else np.zeros(0)
         out[storage] = {"cloud_weight_ms": ms / n, "weights_per_s": weights / (ms / 1e3), "bytes_per_cell": bpc,
                         "gather_bytes_per_s": weights * bpc / (ms / 1e3),
                         "ncu_hall": ncu.get(storage),
-                        "weight_rel_err_vs_fp64": {"max": float(e.max()) if e.size else None,
-                                                   "mean": float(e.mean()) if e.size else None,
-                                                   "particles": int(e.size), "steps": steps}}
+                        "weight_rel_err_vs_fp64": {
+                            "running_sum_max": float(e.max()) if e.size else None,
+                            "running_sum_mean": float(e.mean()) if e.size else None,
+                            "compensated_sum_max": float(ec.max()) if ec.size else None,
+                            "compensated_sum_mean": float(ec.mean()) if ec.size else None,
+                            "particles": int(e.size), "steps": steps,
+                            "note": "running sum: the reference's float sum in cloud order (computeCloudWeight); "
+                                    "compensated: AMCL_OPT_CLOUD_SUM=1 (normalised weights of the sample, "
+                                    "within 2x the per-particle error)"}}
     G.set_storage("f32")
     return out
 
