@@ -402,3 +402,47 @@ def test_normal_draws_statistics(amcl):
     z = pf.draws()[1:].ravel().astype(np.float64)
     assert abs(z.mean()) < 0.01 and abs(z.std() - 1.0) < 0.01
     assert abs((np.abs(z) < 1).mean() - 0.6827) < 0.005
+
+
+def floor_constants_fit(size):
+    """Whether the grid gets floor constants (the host's solve, restated): offsets m of
+    2^23 with sum_a (0x4B000000 + m[a]) * stride[a] = 0 mod 2^32, each leaving room for
+    size[a] + 2 cells below 2^23."""
+    sx, sy, sz = size
+    two32, b = 1 << 32, 0x4B000000
+    r = (two32 - (b * ((1 + sx + sx * sy) % two32)) % two32) % two32
+    m2, r2 = divmod(r, sx * sy)
+    m1, m0 = divmod(r2, sx)
+    return all(m + n + 2 <= (1 << 23) for m, n in zip((m0, m1, m2), size))
+
+
+@pytest.mark.parametrize("dims,fast", [((10, 11, 10), False), ((44, 40, 16), True)],
+                         ids=["no-floor-constants", "floor-constants"])
+def test_cloud_weights_both_yaw_loops(amcl, dims, fast):
+    """The one-thread-per-particle yaw-only weighting on a grid that has floor constants
+    (the loop that takes the cell index from the floor bits and gathers a zero pad cell
+    for rejected points) and on one too small to have them (10 x 11 x 10 cells: the
+    constants' offsets would not fit below 2^23), 65,536 particles each, random cell
+    probabilities and scan points inside and outside the grid, against the oracle."""
+    rng = np.random.default_rng(sum(dims))
+    res = 0.05
+    mn = (0.0, 0.0, 0.0)
+    mx = tuple(d * res for d in dims)
+    size = tuple(int(v) for v in O.grid_sizes(mn, mx, res))
+    assert size == dims and floor_constants_fit(size) == fast
+    cells = int(np.prod(size))
+    prob = rng.uniform(0.0, 8.0, cells).astype(np.float32)
+    dist = rng.uniform(0.0, 1.0, cells).astype(np.float32)
+    G = amcl.Grid3d()
+    G.load_cells({"min": mn, "max": mx, "size": size, "resolution": res, "sensor_dev": 0.05}, dist, prob)
+    centre = np.array(mx) / 2
+    poses = np.zeros((65536, 4), np.float32)
+    poses[:, :3] = centre + rng.uniform(-0.1, 0.1, (65536, 3))
+    poses[:, 3] = rng.uniform(-3.2, 3.2, 65536)
+    scan = np.zeros((700, 4), np.float32)
+    scan[:, :3] = rng.uniform(-0.7, 0.7, (700, 3)) * np.array(mx) / max(mx)
+    w_gpu = G.computeCloudWeights(poses, scan)
+    g = O.GridData(mn, mx, res, size, prob, dist)
+    want = O.cloud_weights(g, poses, scan, 0.0, 0.0, yaw_trig=1)
+    assert (want > 0).mean() > 0.5  # most particles keep more than 10 points
+    np.testing.assert_array_equal(w_gpu, want)
