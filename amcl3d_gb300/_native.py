@@ -127,6 +127,8 @@ _SIGS = {
     "amcl_server_close_session": [_vp, _i64],
     "amcl_server_submit": [_vp, _i64, _fp, _u32, _u32, _fp, _u32, _dp, _d, _d, _d, _d, _int, C.POINTER(_u64)],
     "amcl_server_poll": [_vp, _vp, _u32, C.POINTER(_u32)],
+    "amcl_batch_counters": [_vp, C.POINTER(_u64), C.POINTER(_u64), C.POINTER(_u64)],
+    "amcl_server_counters": [_vp, C.POINTER(_u64), C.POINTER(_u64)],
     "amcl_server_stats": [_vp, C.POINTER(_u64), C.POINTER(_u64), C.POINTER(_d), C.POINTER(_u32), C.POINTER(_u32)],
     "amcl_server_batch": [_vp, C.POINTER(_vp)],
     "amcl_pf_profile": [_vp, _int],

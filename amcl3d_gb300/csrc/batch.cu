@@ -550,16 +550,83 @@ struct Branches
   }
 };
 
+// The batch's own stream-ordered memory pool (allocations that grow while the
+// batch runs come from it, so growing waits only on the batch's stream; a cudaFree
+// would synchronise the whole device, every other batch and server lane included).
+struct PoolHolder
+{
+  cudaMemPool_t pool = nullptr;
+  int init()
+  {
+    int dev = 0;
+    AMCL_CUDA_TRY(cudaGetDevice(&dev));
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    AMCL_CUDA_TRY(cudaMemPoolCreate(&pool, &props));
+    uint64_t keep = UINT64_MAX;  // keep freed memory in the pool for the next growth
+    AMCL_CUDA_TRY(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    return AMCL_OK;
+  }
+  ~PoolHolder()
+  {
+    if (pool)
+      cudaMemPoolDestroy(pool);  // released once the buffers' stream-ordered frees have run
+  }
+};
+
+// A device buffer allocated and freed in stream order from a PoolHolder's pool.
+struct StreamBuf
+{
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaMemPool_t pool = nullptr;
+  cudaStream_t s = nullptr;
+  int ensure(size_t want)
+  {
+    if (want <= bytes && p)
+      return AMCL_OK;
+    if (p)
+      AMCL_CUDA_TRY(cudaFreeAsync(p, s));
+    p = nullptr;
+    bytes = 0;
+    if (want == 0)
+      return AMCL_OK;
+    const cudaError_t e = cudaMallocFromPoolAsync(&p, want, pool, s);
+    if (e != cudaSuccess)
+    {
+      p = nullptr;
+      return fail(AMCL_ENOMEM, std::string("cudaMallocFromPoolAsync ") + std::to_string(want) + " B: " +
+                                   cudaGetErrorString(e));
+    }
+    bytes = want;
+    return AMCL_OK;
+  }
+  template <typename T>
+  T* as() const
+  {
+    return static_cast<T*>(p);
+  }
+  ~StreamBuf()
+  {
+    if (p)
+      cudaFreeAsync(p, s);
+  }
+};
+
 struct amcl_batch_s
 {
   StreamHolder st;
   Branches br;
+  PoolHolder mem;  // declared before the StreamBufs: destroyed after them
   uint32_t max_filters = 0;
   uint64_t max_particles = 0, max_points = 0;
   std::vector<BatchSlot> slots;
   std::vector<std::pair<uint64_t, uint64_t>> free_ranges;  // particle arena [off, len)
   DevBuf pose[2], w[2], wp[2], wr[2], inmap, hi, blocksum, acc, stats, cloud, ranges, steps, counts, blk_items,
-      wt_items, counter, xf, scratch, tile_done;
+      wt_items, counter;
+  StreamBuf xf, scratch, tile_done;  // the split path's, sized by the steps as they come
   PinnedBuf h_cloud, h_ranges, h_steps, h_counts, h_blk, h_wt, h_stats;
   uint32_t n_steps = 0, n_blk = 0, n_wt = 0;
   uint64_t class_mask = 0;  // weighting queues of the packed step: bit q fused queue q, bit 32 + c split class c
@@ -600,6 +667,7 @@ struct amcl_batch_s
   }
   bool in_flight = false;
   uint64_t steps_done = 0;
+  uint64_t graphs_built = 0, reallocs = 0;  // amcl_batch_counters
   std::mutex mu;
   ~amcl_batch_s() { drop_graphs(); }
 };
@@ -910,11 +978,12 @@ void assign_grid_slots(amcl_batch_s* b, SlotStep* hs, const std::vector<const am
 // `cap`): a workload that creeps upwards reallocates, and so frees (a device-wide
 // synchronisation) and drops the captured graphs, only a few times.
 template <typename Buf>
-int grow(Buf& buf, size_t need, size_t cap = SIZE_MAX)
+int grow(amcl_batch_s* b, Buf& buf, size_t need, size_t cap = SIZE_MAX, size_t first = 1u << 20)
 {
   if (buf.p && need <= buf.bytes)
     return AMCL_OK;
-  const size_t dbl = std::max<size_t>(2 * buf.bytes, 1u << 20);
+  const size_t dbl = std::max<size_t>(2 * buf.bytes, first);
+  b->reallocs += 1;
   return buf.ensure(std::max(need, std::min(dbl, cap)));
 }
 
@@ -1031,8 +1100,12 @@ int plan_split(amcl_batch_s* b, int threads)
   const void* old[3] = { b->xf.p, b->scratch.p, b->tile_done.p };
   const size_t old_tiles = b->tile_done.bytes;
   int rc;
-  if ((rc = grow(b->xf, xo * sizeof(SplitRec))) || (rc = grow(b->scratch, sc * 4, b->scratch_cap)) ||
-      (rc = grow(b->tile_done, tiles * 4)))
+  // first reservations: the transforms and tile counters of as many particles as a split
+  // step can hold (fewer fused tiles than SMs, 512-particle tiles at most), 256 MB of slab
+  const size_t split_p = static_cast<size_t>(device_sm_count()) * SPLIT_BELOW_TILES_PER_SM * 512;
+  if ((rc = grow(b, b->xf, xo * sizeof(SplitRec), SIZE_MAX, split_p * sizeof(SplitRec))) ||
+      (rc = grow(b, b->scratch, sc * 4, b->scratch_cap, std::min<size_t>(b->scratch_cap, 256u << 20))) ||
+      (rc = grow(b, b->tile_done, tiles * 4, SIZE_MAX, split_p / 32 * 4)))
     return rc;
   if (b->tile_done.bytes != old_tiles || b->tile_done.p != old[2])
     AMCL_CUDA_TRY(cudaMemsetAsync(b->tile_done.p, 0, b->tile_done.bytes, b->st.s));
@@ -1163,7 +1236,7 @@ int pack_steps(amcl_batch_s* b)
   if (items * sizeof(uint2) > b->wt_items.bytes)
   {
     b->drop_graphs();
-    if ((rc = grow(b->wt_items, items * sizeof(uint2))) || (rc = grow(b->h_wt, items * sizeof(uint2))))
+    if ((rc = grow(b, b->wt_items, items * sizeof(uint2))) || (rc = grow(b, b->h_wt, items * sizeof(uint2))))
       return rc;
   }
   build_weight_items(b, threads);
@@ -1325,6 +1398,13 @@ extern "C" int amcl_batch_create(amcl_batch_t* out, uint32_t max_filters, uint64
   int rc = b->st.init(stream);
   if (!rc)
     rc = b->br.init();
+  if (!rc)
+    rc = b->mem.init();
+  for (StreamBuf* sb : { &b->xf, &b->scratch, &b->tile_done })
+  {
+    sb->pool = b->mem.pool;
+    sb->s = b->st.s;
+  }
   const uint64_t cap = align256(max_particles) + 256ull * max_filters;  // per-slot alignment slack
   const uint64_t pts = std::max<uint64_t>(max_points_per_step, 1);
   const uint64_t rng = 64ull * max_filters;
@@ -1682,6 +1762,20 @@ extern "C" int amcl_batch_stage_packed(amcl_batch_t b, uint32_t count, const int
   return AMCL_OK;
 }
 
+extern "C" int amcl_batch_counters(amcl_batch_t b, uint64_t* steps, uint64_t* graphs_built, uint64_t* reallocs)
+{
+  if (!b)
+    return fail(AMCL_EINVAL, "amcl_batch_counters: null batch");
+  std::lock_guard<std::mutex> lock(b->mu);
+  if (steps)
+    *steps = b->steps_done;
+  if (graphs_built)
+    *graphs_built = b->graphs_built;
+  if (reallocs)
+    *reallocs = b->reallocs;
+  return AMCL_OK;
+}
+
 extern "C" int amcl_batch_step(amcl_batch_t b)
 {
   if (!b)
@@ -1728,6 +1822,7 @@ extern "C" int amcl_batch_step(amcl_batch_t b)
       return rc;
     }
     b->graphs.push_back(fresh);
+    b->graphs_built += 1;
     G = &b->graphs.back();
   }
   if ((rc = graph_update_copies(b, *G)))

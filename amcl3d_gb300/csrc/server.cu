@@ -442,6 +442,27 @@ extern "C" int amcl_server_stats(amcl_server_t S, uint64_t* steps, uint64_t* req
   return AMCL_OK;
 }
 
+extern "C" int amcl_server_counters(amcl_server_t S, uint64_t* graphs_built, uint64_t* reallocs)
+{
+  if (!S)
+    return amcl::fail(AMCL_EINVAL, "amcl_server_counters: null server");
+  uint64_t g = 0, r = 0;
+  for (auto& L : S->lanes)
+  {
+    uint64_t lg = 0, lr = 0;
+    const int rc = amcl_batch_counters(L.batch, nullptr, &lg, &lr);
+    if (rc)
+      return rc;
+    g += lg;
+    r += lr;
+  }
+  if (graphs_built)
+    *graphs_built = g;
+  if (reallocs)
+    *reallocs = r;
+  return AMCL_OK;
+}
+
 extern "C" int amcl_server_batch(amcl_server_t S, amcl_batch_t* batch)
 {
   if (!S || !batch)

@@ -115,6 +115,11 @@ class Server:
             if n.value < len(self._buf):
                 return out
 
+    def counters(self) -> dict:
+        g, r = C.c_uint64(), C.c_uint64()
+        N.call("amcl_server_counters", self._h, C.byref(g), C.byref(r))
+        return {"graphs_built": g.value, "reallocs": r.value}
+
     def stats(self) -> dict:
         steps, reqs, busy, mb, ns = C.c_uint64(), C.c_uint64(), C.c_double(), C.c_uint32(), C.c_uint32()
         N.call("amcl_server_stats", self._h, C.byref(steps), C.byref(reqs), C.byref(busy), C.byref(mb), C.byref(ns))
@@ -194,6 +199,7 @@ def run_load(server: Server, grids, pools, n_sessions: int, rate_hz: float, dura
         if not try_open(s):
             admission.append(s)
     t0 = time.perf_counter()
+    counters0 = None
     events = []  # (time, kind, sid)
     for sid in list(specs):
         heapq.heappush(events, (t0 + rng.exponential(1.0 / rate_hz), 0, sid))
@@ -213,6 +219,8 @@ def run_load(server: Server, grids, pools, n_sessions: int, rate_hz: float, dura
         now = time.perf_counter()
         if now >= t_end:
             break
+        if counters0 is None and now >= t_meas:
+            counters0 = server.counters()
         # completions
         for (ticket, sid, status, ts, td, mean) in server.poll():
             info = outstanding.pop(ticket, None)
@@ -262,6 +270,8 @@ def run_load(server: Server, grids, pools, n_sessions: int, rate_hz: float, dura
         except N.AmclError:
             pass
     backlog = len(outstanding)
+    counters1 = server.counters()
+    counters0 = counters0 or counters1
     lat = np.array(lat)
     lat_srv = np.array(lat_srv)
     st = server.stats()
@@ -278,6 +288,8 @@ def run_load(server: Server, grids, pools, n_sessions: int, rate_hz: float, dura
         "server_p50_ms": float(np.percentile(lat_srv, 50) * 1e3) if lat_srv.size else None,
         "server_p99_ms": float(np.percentile(lat_srv, 99) * 1e3) if lat_srv.size else None,
         "mean_batch": st["requests"] / max(st["steps"], 1),
+        "graphs_built_measured": counters1["graphs_built"] - counters0["graphs_built"],
+        "reallocs_measured": counters1["reallocs"] - counters0["reallocs"],
         "max_batch": st["max_batch"],
         "admission_waiting": len(admission),
         "dropped_behind": int(dropped),

@@ -337,6 +337,9 @@ int amcl_batch_get_tuning(amcl_batch_t b, int* threads, int* chunk);
 int amcl_batch_autotune(amcl_batch_t b, int reps, int* best_threads, int* best_chunk, double* best_ms);
 /* Largest contiguous free particle range and free slots (admission headroom). */
 int amcl_batch_capacity(amcl_batch_t b, uint64_t* free_particles, uint32_t* free_slots);
+/* Steps launched, CUDA graphs captured and work buffers regrown since creation (each
+ * capture and regrowth is a pause of that batch's stream; any may be NULL). */
+int amcl_batch_counters(amcl_batch_t b, uint64_t* steps, uint64_t* graphs_built, uint64_t* reallocs);
 int amcl_batch_stream(amcl_batch_t b, void** stream);
 
 /* ---- server: many localisation sessions, continuous batching ------------------------------
@@ -378,6 +381,8 @@ int amcl_server_submit(amcl_server_t s, int64_t session, const float* xyz, uint3
 int amcl_server_poll(amcl_server_t s, amcl_server_result* out, uint32_t cap, uint32_t* n);
 int amcl_server_stats(amcl_server_t s, uint64_t* steps, uint64_t* requests, double* busy_s, uint32_t* max_batch,
                       uint32_t* sessions);
+/* amcl_batch_counters summed over the lanes. */
+int amcl_server_counters(amcl_server_t s, uint64_t* graphs_built, uint64_t* reallocs);
 /* The batch of the first lane. */
 int amcl_server_batch(amcl_server_t s, amcl_batch_t* batch);
 
