@@ -172,10 +172,12 @@ constexpr int COUNT_WORDS = SQ_BASE + 2 * N_CLASSES;
 __host__ __device__ inline int weight_class(int storage, int cloud_sum) { return storage * 2 + (cloud_sum ? 1 : 0); }
 __host__ __device__ inline int fused_queue(int cls, int gslot) { return cls * N_GSLOTS + (gslot < 0 ? BATCH_GRIDS : gslot); }
 
-// FS: the slot grid has floor constants (only with PG; set by the launcher).
+// FS: the slot grid has floor constants (only with PG; set by the launcher).  The general
+// yaw loop (FS 2) runs 2 blocks of 256 per SM, whose 128 registers a thread hold it
+// without spilling.
 template <int STORAGE, int SUM, bool PG, int MAXT, int FS = 0>
-__global__ __launch_bounds__(MAXT, MAXT >= 512 ? 1 : 3) void k_b_weight(BatchDev d, GridView gp, uint32_t q,
-                                                                         uint32_t chunk)
+__global__ __launch_bounds__(MAXT, MAXT >= 512 ? 1 : (FS == 2 ? 2 : 3)) void k_b_weight(BatchDev d, GridView gp,
+                                                                                        uint32_t q, uint32_t chunk)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   float4* s_pts = reinterpret_cast<float4*>(smem);
@@ -776,12 +778,18 @@ int launch_fused_class(amcl_batch_s* b, const BatchDev& d, int threads, uint32_t
     if (slot < BATCH_GRIDS)
     {
       const GridView& gv = b->gset.g[slot];
+      const int fv = fast_variant(gv);
       AMCL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &per_sm, gv.fast_idx ? k_b_weight<STORAGE, SUM, true, MAXT, 1> : k_b_weight<STORAGE, SUM, true, MAXT, 0>,
+          &per_sm,
+          fv == 1   ? k_b_weight<STORAGE, SUM, true, MAXT, 1>
+          : fv == 2 ? k_b_weight<STORAGE, SUM, true, MAXT, 2>
+                    : k_b_weight<STORAGE, SUM, true, MAXT, 0>,
           threads, smem));
       const unsigned grid = static_cast<unsigned>(device_sm_count() * std::max(per_sm, 1));
-      if (gv.fast_idx)
+      if (fv == 1)
         k_b_weight<STORAGE, SUM, true, MAXT, 1><<<grid, threads, smem, s>>>(d, gv, static_cast<uint32_t>(q), chunk);
+      else if (fv == 2)
+        k_b_weight<STORAGE, SUM, true, MAXT, 2><<<grid, threads, smem, s>>>(d, gv, static_cast<uint32_t>(q), chunk);
       else
         k_b_weight<STORAGE, SUM, true, MAXT, 0><<<grid, threads, smem, s>>>(d, gv, static_cast<uint32_t>(q), chunk);
     }
@@ -860,7 +868,9 @@ int fused_smem_attr(size_t smem)
       (rc = smem_attr(k_b_weight<STORAGE, SUM, true, 512>, smem)) ||
       (rc = smem_attr(k_b_weight<STORAGE, SUM, false, 512>, smem)) ||
       (rc = smem_attr(k_b_weight<STORAGE, SUM, true, 256, 1>, smem)) ||
-      (rc = smem_attr(k_b_weight<STORAGE, SUM, true, 512, 1>, smem)))
+      (rc = smem_attr(k_b_weight<STORAGE, SUM, true, 512, 1>, smem)) ||
+      (rc = smem_attr(k_b_weight<STORAGE, SUM, true, 256, 2>, smem)) ||
+      (rc = smem_attr(k_b_weight<STORAGE, SUM, true, 512, 2>, smem)))
     return rc;
   return AMCL_OK;
 }

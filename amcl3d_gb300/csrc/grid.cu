@@ -123,6 +123,13 @@ int grid_prepare_view(amcl_grid_s* g)
       hi = std::nextafter(hi, INFINITY);
     v.inv_lo[a] = lo;
     v.inv_hi[a] = in.size[a] < (1u << 21) ? hi : INFINITY;
+    float lo2 = v.inv_res[a], hi2 = v.inv_res[a];
+    while (static_cast<double>(lo2) > ir * (1.0 - std::ldexp(1.0, -21)))
+      lo2 = std::nextafter(lo2, 0.0f);
+    while (static_cast<double>(hi2) < ir * (1.0 + std::ldexp(1.0, -21)))
+      hi2 = std::nextafter(hi2, INFINITY);
+    v.inv_lo2[a] = lo2;
+    v.inv_hi2[a] = hi2;
     v.min[a] = in.min[a];
     v.in_lo[a] = float_ceil(in.min[a]);
     v.in_hi[a] = float_ceil(in.max[a]);
@@ -133,6 +140,10 @@ int grid_prepare_view(amcl_grid_s* g)
   v.step_z = in.size[0] * in.size[1];
   v.cells = g->cells();
   grid_floor_constants(v);
+  v.gen_fast = v.fast_idx;
+  for (int a = 0; a < 3; ++a)
+    if (in.size[a] >= (1u << 20) || v.V[a] != g->tabs_host[v.toff[a] + in.size[a]])
+      v.gen_fast = 0;
   // Pairs (T[k], T[k+1]) per axis, T[size+1] = +inf: one 64-bit load settles a cell.
   std::vector<float2> pairs(g->tabs_host.size());
   for (int a = 0; a < 3; ++a)

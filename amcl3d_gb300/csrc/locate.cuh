@@ -65,6 +65,12 @@ struct GridView
   float mag[3];
   uint32_t pad_cell;  // index of the zero cell stored after the last cell of every prob array
   int fast_idx;       // mag[] exists and pad_cell < 2^32
+  // The yaw-only loop for offsets that are not floats (weigh_chunk_yaw2_gen): 1/res
+  // bracketed 2^-21 relative below and above, wide enough for the float estimate of a
+  // transformed coordinate; usable when every axis's bound V is the threshold of its
+  // last cell (V = T[size], so the cell range decides the bounds) and is below 2^21 cells.
+  float inv_lo2[3], inv_hi2[3];
+  int gen_fast;
 };
 
 // Per-particle constants of the transform.
@@ -226,6 +232,18 @@ __device__ __forceinline__ uint32_t cell_index(const GridView& g, int kx, int ky
   if ((kx | ky | kz) < 0)
     return 0xFFFFFFFFu;
   return static_cast<uint32_t>(kx) + static_cast<uint32_t>(ky) * g.step_y + static_cast<uint32_t>(kz) * g.step_z;
+}
+
+// Loop variant of the fused weighting for a grid (the FS template argument): 1 when
+// every offset is a float (zero minimum) and the floor constants exist, 2 when the
+// minimum is not zero and the general yaw loop's constants exist, else 0.
+__host__ __forceinline__ int fast_variant(const GridView& g)
+{
+  if (!g.fast_idx)
+    return 0;
+  if (g.min[0] == 0.0 && g.min[1] == 0.0 && g.min[2] == 0.0)
+    return 1;
+  return g.gen_fast ? 2 : 0;
 }
 
 // Point-transform modes of the weighting loops.

@@ -29,11 +29,11 @@ using namespace amcl;
 
 namespace
 {
-constexpr int WT_THREADS = 192;  // 6 warps; 4 blocks per SM by registers (80 per thread)
+constexpr int WT_THREADS = 192;  // 6 warps; 4 blocks per SM by registers (80 per thread), 3 (96) in the general yaw loop
 constexpr int WT_CHUNK = 1024;  // points staged per block iteration (16 KB)
 
 template <int STORAGE, int SUM, int TAB, int FS = 0>
-__global__ __launch_bounds__(WT_THREADS, 4) void k_weight_fused(WeightArgs a, GridView g)
+__global__ __launch_bounds__(WT_THREADS, FS == 2 ? 3 : 4) void k_weight_fused(WeightArgs a, GridView g)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   float4* s_pts = reinterpret_cast<float4*>(smem);
@@ -239,14 +239,24 @@ int launch_fused(const WeightArgs& a, const GridView& g, cudaStream_t s)
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     AMCL_CUDA_TRY(cudaFuncSetAttribute(k_weight_fused<STORAGE, SUM, TAB_GLOBAL, 1>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    AMCL_CUDA_TRY(cudaFuncSetAttribute(k_weight_fused<STORAGE, SUM, TAB_SHARED, 2>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    AMCL_CUDA_TRY(cudaFuncSetAttribute(k_weight_fused<STORAGE, SUM, TAB_GLOBAL, 2>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     return static_cast<int>(AMCL_OK);
   });
   if (rc)
     return rc;
-  if (g.fast_idx && tables_staged(g))
-    k_weight_fused<STORAGE, SUM, TAB_SHARED, 1><<<ceil_div(a.P, WT_THREADS), WT_THREADS, smem, s>>>(a, g);
-  else if (g.fast_idx)
-    k_weight_fused<STORAGE, SUM, TAB_GLOBAL, 1><<<ceil_div(a.P, WT_THREADS), WT_THREADS, smem, s>>>(a, g);
+  const int fv = fast_variant(g);
+  const unsigned nb = ceil_div(a.P, WT_THREADS);
+  if (fv == 1 && tables_staged(g))
+    k_weight_fused<STORAGE, SUM, TAB_SHARED, 1><<<nb, WT_THREADS, smem, s>>>(a, g);
+  else if (fv == 1)
+    k_weight_fused<STORAGE, SUM, TAB_GLOBAL, 1><<<nb, WT_THREADS, smem, s>>>(a, g);
+  else if (fv == 2 && tables_staged(g))
+    k_weight_fused<STORAGE, SUM, TAB_SHARED, 2><<<nb, WT_THREADS, smem, s>>>(a, g);
+  else if (fv == 2)
+    k_weight_fused<STORAGE, SUM, TAB_GLOBAL, 2><<<nb, WT_THREADS, smem, s>>>(a, g);
   else if (tables_staged(g))
     k_weight_fused<STORAGE, SUM, TAB_SHARED><<<ceil_div(a.P, WT_THREADS), WT_THREADS, smem, s>>>(a, g);
   else

@@ -10,6 +10,7 @@ namespace amcl
 constexpr int UNROLL = 8;
 constexpr int YAW_UNROLL = 8;  // points per group of the paired yaw-only loop
 constexpr int FAST_UNROLL = 8;  // points per group of the loop with floor constants
+constexpr int GEN_UNROLL = 4;   // points per group of the general yaw loop
 constexpr int MAX_RANGES = 64;
 
 __device__ __forceinline__ float exp_f32_via_f64(float x) { return __double2float_rn(exp(static_cast<double>(x))); }
@@ -208,6 +209,171 @@ __device__ __forceinline__ void weigh_chunk_yaw2_fast(const float4* s_pts, const
   }
 }
 
+// ---- yaw-only loop for offsets that are not floats (GridView::gen_fast) --------------------
+// A map whose minimum is not a float multiple of the coordinates (any real octomap
+// map) gives offsets off = double(t) - min that are not floats, and the reference's
+// X = fl32(double(f) + off) is then no single float add.  With off = H + L (H its float
+// rounding, L the float rounding of the rest) the float estimate v = (f + H) + L lies
+// within 3 * 2^-24 * |v| + 2^-48 * |H| of X; so wherever |v| >= 2^-20 * |H| the
+// reference's cell lies between the floors of v against 1/res bracketed 2^-21 relative
+// below and above (GridView::inv_lo2 / inv_hi2), X has v's sign, and when the two floors
+// agree they are the cell and the bounds of v are those of X (every axis's bound being
+// the threshold of its last cell).  Points near 0 or whose floors disagree take the
+// reference's X from a float two-sum (gen_exact_x), after the group's other points.
+struct PartYawG
+{
+  float2 rx, ry;  // (r00, r10), (r01, r11)
+  float2 h, l;    // (H_x, H_y), (L_x, L_y)
+  float2 zb;      // (2^-20 |H_x|, 2^-20 |H_y|): |v| below it takes the exact path
+  float2 nz;      // (-0.0, -0.0), opaque to the compiler
+  float hz, lz, zbz;
+};
+
+__device__ __forceinline__ PartYawG gen_yaw(const GridView& g, const PartXf& p)
+{
+  PartYawG q;
+  q.rx = make_float2(p.r[0], p.r[3]);
+  q.ry = make_float2(p.r[1], p.r[4]);
+  q.h = make_float2(p.H[0], p.H[1]);
+  q.l = make_float2(p.L[0], p.L[1]);
+  q.zb = make_float2(ldexpf(fabsf(p.H[0]), -20), ldexpf(fabsf(p.H[1]), -20));
+  q.nz = make_float2(g.neg_zero, g.neg_zero);
+  q.hz = p.H[2];
+  q.lz = p.L[2];
+  q.zbz = ldexpf(fabsf(p.H[2]), -20);
+  return q;
+}
+
+// The reference's X = fl32(double(s) + off) on one axis from float arithmetic, with
+// off = H + L + r (|r| <= 2^-48 |H|): Knuth's two-sum gives a + e = s + H exactly, then
+// t = fl(e + L), X = fl(a + t) and the residual w = fl((a - X) + t) (a - X is exact while
+// |a| >= 2^-20 |H|), so (s + off) - X = w within 2^-24 (|w| + |t|) + |r|.  X is the
+// reference's rounding unless |w| lies within twice that of half an ulp of X, X is a
+// power of two, or |a| < 2^-20 |H|: then `amb` is set and the caller takes the double
+// add.
+__device__ __forceinline__ float gen_exact_x(float s, float H, float L, bool& amb)
+{
+  const float a = fadd(s, H);
+  const float bv = fsub(a, s);
+  const float av = fsub(a, bv);
+  const float e = fadd(fsub(s, av), fsub(H, bv));
+  const float t = fadd(e, L);
+  const float X = fadd(a, t);
+  const float w = fadd(fsub(a, X), t);
+  const uint32_t xb = __float_as_uint(X) & 0x7FFFFFFFu;
+  const float half_ulp = __uint_as_float((xb & 0x7F800000u) - (24u << 23));
+  const float margin = fadd(fmul(fadd(fabsf(w), fabsf(t)), 1.1920928955078125e-07f),   // 2^-23
+                            fmul(fabsf(H), 7.105427357601002e-15f));                   // 2^-47
+  amb |= !(fabsf(fsub(fabsf(w), half_ulp)) > margin) | ((xb & 0x007FFFFFu) == 0u) | (xb < 0x0D000000u) |
+         !(fabsf(a) >= fmul(fabsf(H), 9.5367431640625e-07f));                           // 2^-20
+  return X;
+}
+
+// The reference's X on one axis: fl32(double(s) + (double(t) - min)) (Grid3d.cpp:155-157).
+// Out of line, so that the double arithmetic is branched around rather than issued,
+// predicated off, for every open point.
+static __device__ __noinline__ float reference_x(float s, float t, double mn)
+{
+  return __double2float_rn(__dadd_rn(static_cast<double>(s), __dsub_rn(static_cast<double>(t), mn)));
+}
+
+// The reference's cell of a point that the widened floors left open (`near`): X per axis
+// from gen_exact_x, or from the reference's double add where that cannot decide.
+template <int TAB>
+__device__ __forceinline__ uint32_t gen_exact_cell(const GridView& g, const float2* tab, const PartYawG& q, float4 xxyy,
+                                                   float pz0, const float4* pose, uint32_t p, bool& valid)
+{
+  const float2 s01 = __fadd2_rn(__ffma2_rn(make_float2(xxyy.x, xxyy.y), q.rx, q.nz),
+                                __ffma2_rn(make_float2(xxyy.z, xxyy.w), q.ry, q.nz));
+  float s[3] = { s01.x, s01.y, pz0 };
+  bool amb = false;
+  float X[3] = { gen_exact_x(s[0], q.h.x, q.l.x, amb), gen_exact_x(s[1], q.h.y, q.l.y, amb),
+                 gen_exact_x(s[2], q.hz, q.lz, amb) };
+  if (amb)
+  {
+    const float4 t = pose[p];
+    X[0] = reference_x(s[0], t.x, g.min[0]);
+    X[1] = reference_x(s[1], t.y, g.min[1]);
+    X[2] = reference_x(s[2], t.z, g.min[2]);
+  }
+  const int kx = locate_pair<TAB>(X[0], tab, g, 0);
+  const int ky = locate_pair<TAB>(X[1], tab, g, 1);
+  const int kz = locate_pair<TAB>(X[2], tab, g, 2);
+  valid = (kx | ky | kz) >= 0;
+  return static_cast<uint32_t>(kx) + static_cast<uint32_t>(ky) * g.step_y + static_cast<uint32_t>(kz) * g.step_z;
+}
+
+template <int STORAGE, int SUM, int TAB>
+__device__ __forceinline__ void weigh_chunk_yaw2_gen(const float4* s_pts, const float* s_z, uint32_t cnt,
+                                                     const float2* s_tab, const GridView& g, const PartYawG& q,
+                                                     const float4* pose, uint32_t p, CloudSum<SUM>& acc)
+{
+  const float2 mxy = make_float2(g.mag[0], g.mag[1]);
+  const float2 ilo = make_float2(g.inv_lo2[0], g.inv_lo2[1]), ihi = make_float2(g.inv_hi2[0], g.inv_hi2[1]);
+  for (uint32_t k = 0; k < cnt; k += GEN_UNROLL)
+  {
+    float zs[GEN_UNROLL];
+#pragma unroll
+    for (int j = 0; j < GEN_UNROLL; j += 4)
+    {
+      const float4 z4 = *reinterpret_cast<const float4*>(s_z + k + j);
+      zs[j] = z4.x;
+      zs[j + 1] = z4.y;
+      zs[j + 2] = z4.z;
+      zs[j + 3] = z4.w;
+    }
+    uint32_t cell[GEN_UNROLL];
+    uint32_t open = 0;  // points whose floors leave the cell open, fixed after the group
+#pragma unroll
+    for (int j = 0; j < GEN_UNROLL; ++j)
+    {
+      const float4 xxyy = s_pts[k + j];
+      const float2 s01 = __fadd2_rn(__ffma2_rn(make_float2(xxyy.x, xxyy.y), q.rx, q.nz),
+                                    __ffma2_rn(make_float2(xxyy.z, xxyy.w), q.ry, q.nz));
+      const float2 v01 = __fadd2_rn(__fadd2_rn(s01, q.h), q.l);
+      const float vz = fadd(fadd(zs[j], q.hz), q.lz);
+      const float2 lo = __ffma2_rd(v01, ilo, mxy), hi = __ffma2_rd(v01, ihi, mxy);
+      const float loz = __fmaf_rd(vz, g.inv_lo2[2], g.mag[2]), hiz = __fmaf_rd(vz, g.inv_hi2[2], g.mag[2]);
+      const bool near = !(lo.x == hi.x) | !(lo.y == hi.y) | !(loz == hiz) | (fabsf(v01.x) < q.zb.x) |
+                        (fabsf(v01.y) < q.zb.y) | (fabsf(vz) < q.zbz);
+      const bool valid = (__float_as_uint(v01.x) < __float_as_uint(g.V[0])) &
+                         (__float_as_uint(v01.y) < __float_as_uint(g.V[1])) &
+                         (__float_as_uint(vz) < __float_as_uint(g.V[2])) & !near;
+      const uint32_t idx =
+          __float_as_uint(lo.x) + __float_as_uint(lo.y) * g.step_y + __float_as_uint(loz) * g.step_z;
+      acc.n += valid ? 1 : 0;
+      cell[j] = valid ? idx : g.pad_cell;
+      open |= near ? (1u << j) : 0u;
+    }
+    if (open)
+    {
+#pragma unroll
+      for (int j = 0; j < GEN_UNROLL; ++j)
+      {
+        if (open & (1u << j))
+        {
+          bool ok;
+          const uint32_t idx = gen_exact_cell<TAB>(g, s_tab, q, s_pts[k + j], zs[j], pose, p, ok);
+          acc.n += ok ? 1 : 0;
+          cell[j] = ok ? idx : g.pad_cell;
+        }
+      }
+    }
+    float v[GEN_UNROLL];
+#pragma unroll
+    for (int j = 0; j < GEN_UNROLL; ++j)
+      v[j] = gather_prob<STORAGE>(g, cell[j]);
+#pragma unroll
+    for (int j = 0; j < GEN_UNROLL; ++j)
+    {
+      if (SUM == 0)
+        acc.sum = fadd(acc.sum, v[j]);
+      else
+        acc.add_uncounted(v[j]);
+    }
+  }
+}
+
 // Point-parallel weighting (a warp = 32 particles, one per lane, over `npts` staged
 // points from k0): each lane writes its particle's cell probability, or -1 for a
 // point the reference skips, to out[(base + k) * 32] for k < cnt, the
@@ -315,8 +481,10 @@ __device__ __forceinline__ void load_tables(const GridView& g, float2* s_tab)
   }
 }
 
-// FS: the grid has floor constants (GridView::fast_idx, checked by the launcher), so the
-// yaw-only points take weigh_chunk_yaw2_fast.
+// FS (chosen by the launcher, fast_variant): 1 = the grid has floor constants and a zero
+// minimum (every offset a float), so yaw-only warps take weigh_chunk_yaw2_fast; 2 = the
+// grid has the general loop's constants (GridView::gen_fast) and a non-zero minimum, so
+// every yaw-only point takes weigh_chunk_yaw2_gen; 0 = neither.
 // One block of particles [p0, p0 + blockDim) of one filter, one thread per particle
 // over the whole cloud in cloud order (the fused weighting).  The caller has loaded
 // s_tab (when a.N > 0) and s_rg.  s_pts holds `chunk` float4 (a multiple of UNROLL):
@@ -349,6 +517,9 @@ __device__ __forceinline__ void weigh_block(const WeightArgs& a, const GridView&
   PartYaw2 q{};
   if (inm && mode == XF_YAW)
     q = pair_yaw(g, xf);
+  PartYawG qg{};
+  if (FS == 2 && inm && yl)
+    qg = gen_yaw(g, xf);
 
   CloudSum<SUM> acc;
   for (uint32_t base = 0; base < a.N; base += ch)
@@ -373,8 +544,10 @@ __device__ __forceinline__ void weigh_block(const WeightArgs& a, const GridView&
     __syncthreads();
     if (!inm)
       continue;
-    if (FS && mode == XF_YAW)
+    if (FS == 1 && mode == XF_YAW)
       weigh_chunk_yaw2_fast<STORAGE, SUM, TAB, U>(s_pts, s_z, cnt8, s_tab, g, q, acc);
+    else if (FS == 2 && yl)
+      weigh_chunk_yaw2_gen<STORAGE, SUM, TAB>(s_pts, s_z, cnt8, s_tab, g, qg, a.pose, p, acc);
     else if (mode == XF_YAW)
       weigh_chunk_yaw2<STORAGE, SUM, TAB>(s_pts, s_z, cnt8, s_tab, g, q, acc);
     else if (mode == XF_EXACT)

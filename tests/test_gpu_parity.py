@@ -416,31 +416,48 @@ def floor_constants_fit(size):
     return all(m + n + 2 <= (1 << 23) for m, n in zip((m0, m1, m2), size))
 
 
-@pytest.mark.parametrize("dims,fast", [((10, 11, 10), False), ((44, 40, 16), True)],
-                         ids=["no-floor-constants", "floor-constants"])
-def test_cloud_weights_both_yaw_loops(amcl, dims, fast):
-    """The one-thread-per-particle yaw-only weighting on a grid that has floor constants
-    (the loop that takes the cell index from the floor bits and gathers a zero pad cell
-    for rejected points) and on one too small to have them (10 x 11 x 10 cells: the
-    constants' offsets would not fit below 2^23), 65,536 particles each, random cell
-    probabilities and scan points inside and outside the grid, against the oracle."""
-    rng = np.random.default_rng(sum(dims))
+@pytest.mark.parametrize("dims,mn,tail,fast", [
+    ((10, 11, 10), (0.0, 0.0, 0.0), 0.0, False),
+    ((44, 40, 16), (0.0, 0.0, 0.0), 0.0, True),
+    ((44, 40, 16), (-17.35, -9.5, -1.4), 0.0, True),
+    ((44, 40, 16), (-17.35, -9.5, -1.4), 0.4, True),
+], ids=["no-floor-constants", "zero-minimum", "real-minimum", "real-minimum-partial-last-cell"])
+def test_cloud_weights_yaw_loops(amcl, dims, mn, tail, fast):
+    """The one-thread-per-particle yaw-only weighting (65,536 particles, random cell
+    probabilities, scan points inside and outside the grid) against the oracle on each
+    loop: a grid too small for floor constants (10 x 11 x 10 cells: the constants'
+    offsets would not fit below 2^23); a zero minimum (every offset a float: the cell
+    index from the floor bits, a zero pad cell for rejected points); a minimum like a
+    real octomap map's (offsets that are not floats: the float estimate with widened
+    floors, the reference's double add near cell boundaries and near 0); and the same
+    with a partial last cell (the bound then inside a cell: the general path).  A
+    thousand particles at yaw 0 and one x see a point placed to land within a few
+    ulps of 0 on x, where only the double add decides the side."""
+    rng = np.random.default_rng(sum(dims) + int(tail * 10) + int(abs(mn[0]) > 0))
     res = 0.05
-    mn = (0.0, 0.0, 0.0)
-    mx = tuple(d * res for d in dims)
+    full = tuple(d - (1 if tail else 0) for d in dims)
+    mx = tuple(mn[a] + (full[a] + tail) * res for a in range(3))
     size = tuple(int(v) for v in O.grid_sizes(mn, mx, res))
-    assert size == dims and floor_constants_fit(size) == fast
+    assert size == dims
+    assert floor_constants_fit(size) == fast
     cells = int(np.prod(size))
     prob = rng.uniform(0.0, 8.0, cells).astype(np.float32)
     dist = rng.uniform(0.0, 1.0, cells).astype(np.float32)
     G = amcl.Grid3d()
     G.load_cells({"min": mn, "max": mx, "size": size, "resolution": res, "sensor_dev": 0.05}, dist, prob)
-    centre = np.array(mx) / 2
-    poses = np.zeros((65536, 4), np.float32)
-    poses[:, :3] = centre + rng.uniform(-0.1, 0.1, (65536, 3))
-    poses[:, 3] = rng.uniform(-3.2, 3.2, 65536)
+    centre = (np.array(mn) + np.array(mx)) / 2
+    ext = np.array(mx) - np.array(mn)
+    P = 65536
+    poses = np.zeros((P, 4), np.float32)
+    poses[:, :3] = centre + rng.uniform(-0.1, 0.1, (P, 3))
+    poses[:, 3] = rng.uniform(-3.2, 3.2, P)
+    poses[:1000, 3] = 0.0
+    poses[:1000, 0] = np.float32(centre[0] + 0.0137)
     scan = np.zeros((700, 4), np.float32)
-    scan[:, :3] = rng.uniform(-0.7, 0.7, (700, 3)) * np.array(mx) / max(mx)
+    scan[:, :3] = rng.uniform(-0.7, 0.7, (700, 3)) * ext / ext.max()
+    # the point that lands at ~0 on x for the first thousand particles: x = -fl32(t_x - min_x)
+    h = np.float32(float(poses[0, 0]) - mn[0])
+    scan[5, 0] = -h
     w_gpu = G.computeCloudWeights(poses, scan)
     g = O.GridData(mn, mx, res, size, prob, dist)
     want = O.cloud_weights(g, poses, scan, 0.0, 0.0, yaw_trig=1)
