@@ -100,6 +100,25 @@ def make_workload(cfg: dict, seed: int):
     return occ_points, info, scans, ranges, odos, parts
 
 
+def shift_workload(workload, shift):
+    """The workload with its map, particles and beacon anchors moved by `shift` (metres);
+    the scans are in the sensor frame and stay as they are."""
+    occ, info, scans, ranges, odos, parts = workload
+    sh = np.asarray(shift, np.float64)
+    info = dict(info)
+    info["min"] = tuple(float(a + b) for a, b in zip(info["min"], sh))
+    info["max"] = tuple(float(a + b) for a, b in zip(info["max"], sh))
+    occ = (occ.astype(np.float64) + sh).astype(np.float32)
+    parts = parts.copy()
+    parts[:, :3] = (parts[:, :3].astype(np.float64) + sh).astype(np.float32)
+    moved = []
+    for rg in ranges:
+        r = rg.copy()
+        r[:, 1:4] = (r[:, 1:4].astype(np.float64) + sh).astype(np.float32)
+        moved.append(r)
+    return occ, info, scans, moved, odos, parts
+
+
 # ---- clocks sampled during the timed region --------------------------------------------------------
 
 class ClockSampler:
@@ -404,7 +423,8 @@ def run_ours(args, cfg, rank, world, local_rank):
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     seed = 1000 + rank
-    ft = FilterTiming(cfg, seed, dev)
+    ft = FilterTiming(cfg, seed, dev,
+                      workload=shift_workload(make_workload(cfg, seed), args.map_shift) if args.map_shift else None)
     log(f"[rank {rank}] grid {ft.info['dims']} built on the GPU in {ft.build_s:.2f}s")
     if args.storage != "f32":
         ft.G.set_storage(args.storage)  # the headline filter gathers the narrower cells
@@ -423,7 +443,7 @@ def run_ours(args, cfg, rank, world, local_rank):
     alg_bytes = P * N_mean * 4 + 28 * P + 16 * N_mean + 16 * cfg["B"] * P
     cw_launch_ms = cw_ms / cw_n if cw_n else None
     achieved = alg_bytes / (cw_launch_ms / 1e3) / 1e9 if cw_n else None
-    issue = load_issue_profile(args.config)
+    issue = None if args.map_shift else load_issue_profile(args.config)  # profiled on the zero-minimum map
     res = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
@@ -434,7 +454,7 @@ def run_ours(args, cfg, rank, world, local_rank):
         "e2e": {"value": e2e_total / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(r["launches"]),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None, "traffic": load_traffic(args.config),
+                     "frac": (achieved / peak) if achieved else None, "traffic": None if args.map_shift else load_traffic(args.config),
                      "peak_source": peak_kind, "kernel": "cloud weight (per-particle scan gather)",
                      "kernel_ms_per_launch": cw_launch_ms,
                      "traffic_unit": "DRAM bytes per launch (ncu)",
@@ -444,6 +464,8 @@ def run_ours(args, cfg, rank, world, local_rank):
         "kernel_ms": {k: (v[0] / v[1] if v[1] else None) for k, v in prof.items()},
         "clocks": r["clocks"],
     }
+    if args.map_shift:
+        res["config"]["map_minimum"] = ft.info["min"]
     if issue and cw_launch_ms:
         # the issue-side roof: warp instructions per particle x point (ncu) at the SMs'
         # full issue rate (one warp instruction per cycle per scheduler, 4 per SM)
@@ -468,6 +490,7 @@ def run_ours(args, cfg, rank, world, local_rank):
         res["voxel_filter"] = voxel_section(seed + 5)
         res["grid_storage"] = storage_section(ft, seed, g_host)
         res["distance_field"] = distance_field_section(ft, seed)
+        res["map_minimum"] = map_minimum_section(ft, seed, prof)
         del g_host
         res["room"] = room_section(seed + 3, dev)
         if args.served_sessions > 0:
@@ -580,6 +603,28 @@ def distance_field_section(ft, seed):
                                         "the sub-block's bounds is slow: all 22.8 M occupied points lie outside "
                                         "it and are bucketed into its edge buckets (exact, but every edge cell "
                                         "scans them)"}}
+
+
+def map_minimum_section(ft, seed, zero_min_prof, steps=5, warmup=3, shift=(-17.35, -9.5, -1.4)):
+    """The headline filter on its map moved so that the minimum is not zero, as a real
+    octomap map's bounds are: the offsets double(t) - min are then no floats, and the cloud
+    weighting takes the general yaw loop.  The same scans, particles and steps, the map,
+    particles and beacon anchors moved by `shift`; cloud-weighting ms per launch against
+    the headline's (zero minimum)."""
+    import torch
+
+    wl = shift_workload((ft.occ, ft.info, ft.scans, ft.ranges, ft.odos, ft.parts), shift)
+    moved = FilterTiming(ft.cfg, seed, ft.dev, workload=wl)
+    r = moved.run(steps, warmup)
+    cw_ms, cw_n = r["prof"]["cloud_weight"]
+    z_ms, z_n = zero_min_prof["cloud_weight"]
+    out = {"minimum": wl[1]["min"], "cloud_weight_ms_per_launch": cw_ms / cw_n,
+           "zero_minimum_ms_per_launch": z_ms / z_n, "ratio_to_zero_minimum": (cw_ms / cw_n) / (z_ms / z_n),
+           "weights_per_s": r["weights"] / (r["ms"] / 1e3), "steps": steps,
+           "loop": "general yaw loop: float estimate, floors widened 2^-21, float two-sum for open points"}
+    del moved
+    torch.cuda.empty_cache()
+    return out
 
 
 def four_maps(ft, seed):
@@ -1024,6 +1069,9 @@ def main():
     ap.add_argument("--lanes", type=int, default=4, help="served config: concurrent server lanes")
     ap.add_argument("--storage", choices=["f32", "f16", "u8"], default="f32",
                     help="grid storage the headline filter (or the served config) gathers")
+    ap.add_argument("--map-shift", type=lambda t: tuple(float(v) for v in t.split(",")), default=None,
+                    help="dx,dy,dz: move the map (and particles, beacons) so that its minimum is not zero, as a "
+                         "real map's is; the cloud weighting then takes the general yaw loop")
     ap.add_argument("--served-sessions", type=int, default=1000,
                     help="sessions of the served section of the default line (0: skip the batched, small-filter "
                          "and served sections)")

@@ -28,3 +28,31 @@ def test_sparse_reference_grid_gives_the_same_update():
     touched = np.flatnonzero(sparse.prob)
     assert touched.size < sparse.prob.size
     np.testing.assert_array_equal(sparse.prob[touched], full.prob[touched])
+
+
+def test_shift_workload_moves_map_particles_and_anchors():
+    """`--map-shift` (and the default line's `map_minimum` section) move the map, the
+    particles and the beacon anchors; the scans stay in the sensor frame."""
+    m = S.make_map(23, size_m=(6.0, 5.0, 3.0), n_boxes=6)
+    info = dict(min=m.min, max=m.max, res=m.res, dims=m.dims, n_points=int(m.points.shape[0]))
+    pose = S.free_pose(m, 24, height=1.2, clearance=0.4)
+    scans = [S.ray_cast(m, pose, n_max=300, max_range=6.0, seed=25)]
+    ranges = [S.beacons(m, pose, 3, seed=26)]
+    odos = [S.odometry_step(27)]
+    parts = S.particles_around(pose, 50, 28)
+    sh = (-17.35, -9.5, -1.4)
+    occ2, info2, scans2, ranges2, odos2, parts2 = bench.shift_workload(
+        (m.points, info, scans, ranges, odos, parts), sh)
+    np.testing.assert_allclose(info2["min"], np.asarray(m.min) + sh)
+    np.testing.assert_allclose(info2["max"], np.asarray(m.max) + sh)
+    assert info2["res"] == info["res"] and info2["dims"] == info["dims"] and info["min"] == m.min
+    np.testing.assert_allclose(occ2, m.points.astype(np.float64) + sh, atol=1e-5)
+    np.testing.assert_allclose(parts2[:, :3], parts[:, :3].astype(np.float64) + sh, atol=1e-5)
+    np.testing.assert_array_equal(parts2[:, 3:], parts[:, 3:])
+    np.testing.assert_array_equal(ranges2[0][:, 0], ranges[0][:, 0])
+    np.testing.assert_allclose(ranges2[0][:, 1:4], ranges[0][:, 1:4].astype(np.float64) + sh, atol=1e-5)
+    assert scans2[0] is scans[0] and odos2[0] is odos[0]
+    # every occupied voxel keeps its cell: floor((p - min) / res) is unchanged by the move
+    k0 = np.floor((m.points.astype(np.float64) - np.asarray(m.min)) / m.res)
+    k1 = np.floor((occ2.astype(np.float64) - np.asarray(info2["min"])) / m.res)
+    np.testing.assert_array_equal(k0, k1)
