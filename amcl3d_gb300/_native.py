@@ -69,6 +69,7 @@ _SIGS = {
     "amcl_grid_save": [_vp, C.c_char_p],
     "amcl_grid_load": [_vp, C.c_char_p, _dp, _dp, _d, _d],
     "amcl_grid_info_get": [_vp, C.POINTER(GridInfo)],
+    "amcl_grid_weight_loop": [_vp, C.POINTER(_int)],
     "amcl_grid_read_cells": [_vp, _u64, _u64, _fp, _fp],
     "amcl_grid_set_storage": [_vp, _int],
     "amcl_grid_set_l2_window": [_vp, _int],

@@ -729,6 +729,16 @@ extern "C" int amcl_grid_info_get(amcl_grid_t g, amcl_grid_info* out)
   return AMCL_OK;
 }
 
+extern "C" int amcl_grid_weight_loop(amcl_grid_t g, int* loop)
+{
+  if (!g || !loop)
+    return fail(AMCL_EINVAL, "amcl_grid_weight_loop: bad arguments");
+  if (!g->built)
+    return fail(AMCL_ESTATE, "amcl_grid_weight_loop: grid not built");
+  *loop = fast_variant(g->view);
+  return AMCL_OK;
+}
+
 extern "C" int amcl_grid_read_cells(amcl_grid_t g, uint64_t first, uint64_t count, float* dist, float* prob)
 {
   if (!g)

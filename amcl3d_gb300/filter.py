@@ -142,6 +142,13 @@ class Grid3d:
         N.call("amcl_grid_read_cells", self._h, first, count, N.fptr(d), N.fptr(p))
         return d, p
 
+    def weight_loop(self) -> int:
+        """The yaw-only weighting loop the grid selects: 0 general, 1 zero minimum (offsets
+        are floats), 2 general yaw loop (a real map's minimum)."""
+        v = C.c_int()
+        N.call("amcl_grid_weight_loop", self._h, C.byref(v))
+        return int(v.value)
+
     def set_storage(self, storage: str | int) -> None:
         code = {"f32": N.GRID_F32, "f16": N.GRID_F16, "u8": N.GRID_U8}.get(storage, storage)
         N.call("amcl_grid_set_storage", self._h, int(code))

@@ -104,6 +104,13 @@ int amcl_grid_read_cells(amcl_grid_t g, uint64_t first, uint64_t count, float* d
  * F32 probabilities on first use). */
 int amcl_grid_set_storage(amcl_grid_t g, int storage);
 
+/* The yaw-only cloud-weighting loop this grid selects (no reference counterpart; the
+ * cells are the same on every loop): 0 = the general loop (a float-float estimate with a
+ * margin test per point), 1 = the zero-minimum loop (every offset double(t) - min is a
+ * float: the cell index read off the floor bits), 2 = the general yaw loop for a minimum
+ * that makes the offsets non-floats (a real map's).  AMCL_ESTATE if not built. */
+int amcl_grid_weight_loop(amcl_grid_t g, int* loop);
+
 /* Keeps the gathered probability array in an L2 persisting access-policy window on
  * this grid's stream and on the streams of filters that use it (0 = off, default). */
 int amcl_grid_set_l2_window(amcl_grid_t g, int enable);

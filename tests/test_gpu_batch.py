@@ -160,17 +160,25 @@ def test_batch_more_grids_than_slots(amcl):
     """Six filters on six maps in one batch: four grids ride in the launch's grid slots,
     two are read from their step descriptors.  Then three filters move to two other maps
     (free slots are reused, the captured graphs rebuilt) and two maps no filter uses are
-    destroyed.  Every filter steps exactly as the same filter stepped alone over the same
-    maps."""
+    destroyed.  Three of the maps sit at a minimum like a real octomap map's (offsets that
+    are not floats: the general yaw loop).  Every filter steps exactly as the same filter
+    stepped alone over the same maps."""
     import gc
 
     from amcl3d_gb300.batch import FilterBatch
 
     maps = [S.make_map(80 + k, size_m=(6.0 + k, 5.0, 3.0), n_boxes=6) for k in range(8)]
+    shifts = {2: (-3.35, -1.15, -0.45), 3: (-17.35, -9.5, -1.4), 5: (-0.35, -2.7, -0.15)}  # filters 2, 3, 5 stay
+
+    def moved(k, xyz):  # map-local coordinates into map k's frame
+        return (np.asarray(xyz, np.float64) + np.asarray(shifts.get(k, (0.0, 0.0, 0.0)))).astype(np.float32)
+
     grids = []
-    for m in maps:
+    for k, m in enumerate(maps):
         G = amcl.Grid3d()
-        assert G.buildGridMap(m.points, m.min, m.max, m.res, S.SENSOR_DEV)
+        assert G.buildGridMap(moved(k, m.points), tuple(np.asarray(m.min) + shifts.get(k, (0.0, 0.0, 0.0))),
+                              tuple(np.asarray(m.max) + shifts.get(k, (0.0, 0.0, 0.0))), m.res, S.SENSOR_DEV)
+        assert G.weight_loop() == (2 if k in shifts else 1)
         grids.append(G)
     odom = (*MODS, 0.05, 0.01, 0.0, 0.02)
     moves = {0: 6, 1: 7, 4: 6}  # filter -> map from step 2 on
@@ -181,8 +189,11 @@ def test_batch_more_grids_than_slots(amcl):
         poses = [pose if g == k else S.free_pose(maps[g], 7 + k, height=1.2, clearance=0.4) for g in seq]
         scans = [S.ray_cast(maps[g], q, n_max=600, max_range=6.0, seed=99 + k + 10 * s)
                  for s, (g, q) in enumerate(zip(seq, poses))]
-        specs.append(dict(seq=seq, P=1000 + 700 * k, seed=500 + k, parts=S.particles_around(pose, 1000 + 700 * k, 95 + k),
-                          scans=scans, ranges=S.beacons(maps[k], pose, 3, seed=120 + k)))
+        parts = S.particles_around(pose, 1000 + 700 * k, 95 + k)
+        parts[:, :3] = moved(k, parts[:, :3])
+        ranges = S.beacons(maps[k], pose, 3, seed=120 + k)
+        ranges[:, 1:4] = moved(k, ranges[:, 1:4])
+        specs.append(dict(seq=seq, P=1000 + 700 * k, seed=500 + k, parts=parts, scans=scans, ranges=ranges))
     alone = []
     for sp in specs:
         pf = amcl.ParticleFilter(seed=sp["seed"])

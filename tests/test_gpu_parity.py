@@ -416,13 +416,13 @@ def floor_constants_fit(size):
     return all(m + n + 2 <= (1 << 23) for m, n in zip((m0, m1, m2), size))
 
 
-@pytest.mark.parametrize("dims,mn,tail,fast", [
-    ((10, 11, 10), (0.0, 0.0, 0.0), 0.0, False),
-    ((44, 40, 16), (0.0, 0.0, 0.0), 0.0, True),
-    ((44, 40, 16), (-17.35, -9.5, -1.4), 0.0, True),
-    ((44, 40, 16), (-17.35, -9.5, -1.4), 0.4, True),
+@pytest.mark.parametrize("dims,mn,tail,fast,loop", [
+    ((10, 11, 10), (0.0, 0.0, 0.0), 0.0, False, 0),
+    ((44, 40, 16), (0.0, 0.0, 0.0), 0.0, True, 1),
+    ((44, 40, 16), (-17.35, -9.5, -1.4), 0.0, True, 2),
+    ((44, 40, 16), (-17.35, -9.5, -1.4), 0.4, True, 0),
 ], ids=["no-floor-constants", "zero-minimum", "real-minimum", "real-minimum-partial-last-cell"])
-def test_cloud_weights_yaw_loops(amcl, dims, mn, tail, fast):
+def test_cloud_weights_yaw_loops(amcl, dims, mn, tail, fast, loop):
     """The one-thread-per-particle yaw-only weighting (65,536 particles, random cell
     probabilities, scan points inside and outside the grid) against the oracle on each
     loop: a grid too small for floor constants (10 x 11 x 10 cells: the constants'
@@ -445,6 +445,7 @@ def test_cloud_weights_yaw_loops(amcl, dims, mn, tail, fast):
     dist = rng.uniform(0.0, 1.0, cells).astype(np.float32)
     G = amcl.Grid3d()
     G.load_cells({"min": mn, "max": mx, "size": size, "resolution": res, "sensor_dev": 0.05}, dist, prob)
+    assert G.weight_loop() == loop
     centre = (np.array(mn) + np.array(mx)) / 2
     ext = np.array(mx) - np.array(mn)
     P = 65536
