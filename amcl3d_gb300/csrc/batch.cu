@@ -176,7 +176,8 @@ __host__ __device__ inline int fused_queue(int cls, int gslot) { return cls * N_
 // yaw loop (FS 2) runs 2 blocks of 256 per SM, whose 128 registers a thread hold it
 // without spilling.
 template <int STORAGE, int SUM, bool PG, int MAXT, int FS = 0>
-__global__ __launch_bounds__(MAXT, MAXT >= 512 ? 1 : (FS == 2 ? 2 : 3)) void k_b_weight(BatchDev d, GridView gp,
+__global__ __launch_bounds__(MAXT, MAXT >= 512 ? 1 : (FS == 2 ? 2 : 3)) void k_b_weight(BatchDev d,
+                                                                                        const __grid_constant__ GridView gp,
                                                                                         uint32_t q, uint32_t chunk)
 {
   extern __shared__ __align__(16) unsigned char smem[];

@@ -29,11 +29,11 @@ using namespace amcl;
 
 namespace
 {
-constexpr int WT_THREADS = 192;  // 6 warps; 4 blocks per SM by registers (80 per thread), 3 (96) in the general yaw loop
+constexpr int WT_THREADS = 192;  // 6 warps; 4 blocks per SM by registers (80 per thread)
 constexpr int WT_CHUNK = 1024;  // points staged per block iteration (16 KB)
 
 template <int STORAGE, int SUM, int TAB, int FS = 0>
-__global__ __launch_bounds__(WT_THREADS, FS == 2 ? 3 : 4) void k_weight_fused(WeightArgs a, GridView g)
+__global__ __launch_bounds__(WT_THREADS, 4) void k_weight_fused(WeightArgs a, const __grid_constant__ GridView g)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   float4* s_pts = reinterpret_cast<float4*>(smem);

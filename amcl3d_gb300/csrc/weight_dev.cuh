@@ -277,29 +277,31 @@ static __device__ __noinline__ float reference_x(float s, float t, double mn)
   return __double2float_rn(__dadd_rn(static_cast<double>(s), __dsub_rn(static_cast<double>(t), mn)));
 }
 
-// The reference's cell of a point that the widened floors left open (`near`): X per axis
-// from gen_exact_x, or from the reference's double add where that cannot decide.
+// The reference's cell of a point that the widened floors left open (`near`), or
+// 0xFFFFFFFF where the reference rejects it: X per axis from gen_exact_x, or from the
+// reference's double add where that cannot decide.  Out of line with scalar arguments
+// and the grid by address (a __grid_constant__ kernel parameter), so that the loop
+// around it keeps its registers for the common case.
 template <int TAB>
-__device__ __forceinline__ uint32_t gen_exact_cell(const GridView& g, const float2* tab, const PartYawG& q, float4 xxyy,
-                                                   float pz0, const float4* pose, uint32_t p, bool& valid)
+static __device__ __noinline__ uint32_t open_cell(const GridView* gp, const float2* tab, float sx, float sy, float sz,
+                                                  float hx, float hy, float hz, float lx, float ly, float lz,
+                                                  const float4* pose, uint32_t p)
 {
-  const float2 s01 = __fadd2_rn(__ffma2_rn(make_float2(xxyy.x, xxyy.y), q.rx, q.nz),
-                                __ffma2_rn(make_float2(xxyy.z, xxyy.w), q.ry, q.nz));
-  float s[3] = { s01.x, s01.y, pz0 };
+  const GridView& g = *gp;
   bool amb = false;
-  float X[3] = { gen_exact_x(s[0], q.h.x, q.l.x, amb), gen_exact_x(s[1], q.h.y, q.l.y, amb),
-                 gen_exact_x(s[2], q.hz, q.lz, amb) };
+  float X[3] = { gen_exact_x(sx, hx, lx, amb), gen_exact_x(sy, hy, ly, amb), gen_exact_x(sz, hz, lz, amb) };
   if (amb)
   {
     const float4 t = pose[p];
-    X[0] = reference_x(s[0], t.x, g.min[0]);
-    X[1] = reference_x(s[1], t.y, g.min[1]);
-    X[2] = reference_x(s[2], t.z, g.min[2]);
+    X[0] = reference_x(sx, t.x, g.min[0]);
+    X[1] = reference_x(sy, t.y, g.min[1]);
+    X[2] = reference_x(sz, t.z, g.min[2]);
   }
   const int kx = locate_pair<TAB>(X[0], tab, g, 0);
   const int ky = locate_pair<TAB>(X[1], tab, g, 1);
   const int kz = locate_pair<TAB>(X[2], tab, g, 2);
-  valid = (kx | ky | kz) >= 0;
+  if ((kx | ky | kz) < 0)
+    return 0xFFFFFFFFu;
   return static_cast<uint32_t>(kx) + static_cast<uint32_t>(ky) * g.step_y + static_cast<uint32_t>(kz) * g.step_z;
 }
 
@@ -352,8 +354,12 @@ __device__ __forceinline__ void weigh_chunk_yaw2_gen(const float4* s_pts, const 
       {
         if (open & (1u << j))
         {
-          bool ok;
-          const uint32_t idx = gen_exact_cell<TAB>(g, s_tab, q, s_pts[k + j], zs[j], pose, p, ok);
+          const float4 xxyy = s_pts[k + j];
+          const float2 s01 = __fadd2_rn(__ffma2_rn(make_float2(xxyy.x, xxyy.y), q.rx, q.nz),
+                                        __ffma2_rn(make_float2(xxyy.z, xxyy.w), q.ry, q.nz));
+          const uint32_t idx = open_cell<TAB>(&g, s_tab, s01.x, s01.y, zs[j], q.h.x, q.h.y, q.hz, q.l.x, q.l.y,
+                                              q.lz, pose, p);
+          const bool ok = idx != 0xFFFFFFFFu;
           acc.n += ok ? 1 : 0;
           cell[j] = ok ? idx : g.pad_cell;
         }
