@@ -119,7 +119,10 @@ __device__ __forceinline__ void make_partxf(const GridView& g, float sr, float c
     const double off = __dsub_rn(static_cast<double>(t[a]), g.min[a]);  // Grid3d.cpp:155-157
     p.off[a] = off;
     p.H[a] = fadd(__double2float_rn(off), 0.0f);  // -0.0 becomes +0.0: the same cell, never a -0.0 sum
-    p.L[a] = __double2float_rn(__dsub_rn(off, static_cast<double>(p.H[a])));
+    // L = 0 exactly when off is the float H (a rest below the smallest subnormal keeps it)
+    const double rest = __dsub_rn(off, static_cast<double>(p.H[a]));
+    const float L = __double2float_rn(rest);
+    p.L[a] = (L == 0.0f && rest != 0.0) ? copysignf(1.401298464324817e-45f, static_cast<float>(rest)) : L;
   }
   p.exact = (p.off[0] == static_cast<double>(p.H[0]) && p.off[1] == static_cast<double>(p.H[1]) &&
              p.off[2] == static_cast<double>(p.H[2]) && isfinite(p.H[0]) && isfinite(p.H[1]) && isfinite(p.H[2]))

@@ -214,7 +214,7 @@ __device__ __forceinline__ void weigh_chunk_yaw2_fast(const float4* s_pts, const
 // map) gives offsets off = double(t) - min that are not floats, and the reference's
 // X = fl32(double(f) + off) is then no single float add.  With off = H + L (H its float
 // rounding, L the float rounding of the rest) the float estimate v = (f + H) + L lies
-// within 3 * 2^-24 * |v| + 2^-48 * |H| of X; so wherever |v| >= 2^-20 * |H| the
+// within 3.1 * 2^-24 * |v| + 2^-47 * |H| of X; so wherever |v| >= 2^-20 * |H| the
 // reference's cell lies between the floors of v against 1/res bracketed 2^-21 relative
 // below and above (GridView::inv_lo2 / inv_hi2), X has v's sign, and when the two floors
 // agree they are the cell and the bounds of v are those of X (every axis's bound being
@@ -224,9 +224,9 @@ struct PartYawG
 {
   float2 rx, ry;  // (r00, r10), (r01, r11)
   float2 h, l;    // (H_x, H_y), (L_x, L_y)
-  float2 zb;      // (2^-20 |H_x|, 2^-20 |H_y|): |v| below it takes the exact path
+  float zb;       // 2^-20 max_a |H_a|: |v| below it on any axis takes the exact path
   float2 nz;      // (-0.0, -0.0), opaque to the compiler
-  float hz, lz, zbz;
+  float hz, lz;
 };
 
 __device__ __forceinline__ PartYawG gen_yaw(const GridView& g, const PartXf& p)
@@ -236,11 +236,10 @@ __device__ __forceinline__ PartYawG gen_yaw(const GridView& g, const PartXf& p)
   q.ry = make_float2(p.r[1], p.r[4]);
   q.h = make_float2(p.H[0], p.H[1]);
   q.l = make_float2(p.L[0], p.L[1]);
-  q.zb = make_float2(ldexpf(fabsf(p.H[0]), -20), ldexpf(fabsf(p.H[1]), -20));
+  q.zb = ldexpf(fmaxf(fmaxf(fabsf(p.H[0]), fabsf(p.H[1])), fabsf(p.H[2])), -20);
   q.nz = make_float2(g.neg_zero, g.neg_zero);
   q.hz = p.H[2];
   q.lz = p.L[2];
-  q.zbz = ldexpf(fabsf(p.H[2]), -20);
   return q;
 }
 
@@ -250,7 +249,8 @@ __device__ __forceinline__ PartYawG gen_yaw(const GridView& g, const PartXf& p)
 // |a| >= 2^-20 |H|), so (s + off) - X = w within 2^-24 (|w| + |t|) + |r|.  X is the
 // reference's rounding unless |w| lies within twice that of half an ulp of X, X is a
 // power of two, or |a| < 2^-20 |H|: then `amb` is set and the caller takes the double
-// add.
+// add.  L = 0 means off is the float H (make_partxf keeps L nonzero otherwise): then X is
+// a = fl(s + H), which is fl32(fl64(s + H)) (ties included), and nothing is undecided.
 __device__ __forceinline__ float gen_exact_x(float s, float H, float L, bool& amb)
 {
   const float a = fadd(s, H);
@@ -264,8 +264,8 @@ __device__ __forceinline__ float gen_exact_x(float s, float H, float L, bool& am
   const float half_ulp = __uint_as_float((xb & 0x7F800000u) - (24u << 23));
   const float margin = fadd(fmul(fadd(fabsf(w), fabsf(t)), 1.1920928955078125e-07f),   // 2^-23
                             fmul(fabsf(H), 7.105427357601002e-15f));                   // 2^-47
-  amb |= !(fabsf(fsub(fabsf(w), half_ulp)) > margin) | ((xb & 0x007FFFFFu) == 0u) | (xb < 0x0D000000u) |
-         !(fabsf(a) >= fmul(fabsf(H), 9.5367431640625e-07f));                           // 2^-20
+  amb |= (L != 0.0f) & (!(fabsf(fsub(fabsf(w), half_ulp)) > margin) | ((xb & 0x007FFFFFu) == 0u) |
+                        (xb < 0x0D000000u) | !(fabsf(a) >= fmul(fabsf(H), 9.5367431640625e-07f)));  // 2^-20
   return X;
 }
 
@@ -336,8 +336,8 @@ __device__ __forceinline__ void weigh_chunk_yaw2_gen(const float4* s_pts, const 
       const float vz = fadd(fadd(zs[j], q.hz), q.lz);
       const float2 lo = __ffma2_rd(v01, ilo, mxy), hi = __ffma2_rd(v01, ihi, mxy);
       const float loz = __fmaf_rd(vz, g.inv_lo2[2], g.mag[2]), hiz = __fmaf_rd(vz, g.inv_hi2[2], g.mag[2]);
-      const bool near = !(lo.x == hi.x) | !(lo.y == hi.y) | !(loz == hiz) | (fabsf(v01.x) < q.zb.x) |
-                        (fabsf(v01.y) < q.zb.y) | (fabsf(vz) < q.zbz);
+      const bool near = !(lo.x == hi.x) | !(lo.y == hi.y) | !(loz == hiz) | (fabsf(v01.x) < q.zb) |
+                        (fabsf(v01.y) < q.zb) | (fabsf(vz) < q.zb);
       const bool valid = (__float_as_uint(v01.x) < __float_as_uint(g.V[0])) &
                          (__float_as_uint(v01.y) < __float_as_uint(g.V[1])) &
                          (__float_as_uint(vz) < __float_as_uint(g.V[2])) & !near;

@@ -421,7 +421,8 @@ def floor_constants_fit(size):
     ((44, 40, 16), (0.0, 0.0, 0.0), 0.0, True, 1),
     ((44, 40, 16), (-17.35, -9.5, -1.4), 0.0, True, 2),
     ((44, 40, 16), (-17.35, -9.5, -1.4), 0.4, True, 0),
-], ids=["no-floor-constants", "zero-minimum", "real-minimum", "real-minimum-partial-last-cell"])
+    ((44, 40, 16), (-9.5, -4.25, -1.5), 0.0, True, 2),
+], ids=["no-floor-constants", "zero-minimum", "real-minimum", "real-minimum-partial-last-cell", "float-minimum"])
 def test_cloud_weights_yaw_loops(amcl, dims, mn, tail, fast, loop):
     """The one-thread-per-particle yaw-only weighting (65,536 particles, random cell
     probabilities, scan points inside and outside the grid) against the oracle on each
@@ -430,7 +431,8 @@ def test_cloud_weights_yaw_loops(amcl, dims, mn, tail, fast, loop):
     index from the floor bits, a zero pad cell for rejected points); a minimum like a
     real octomap map's (offsets that are not floats: the float estimate with widened
     floors, the reference's double add near cell boundaries and near 0); and the same
-    with a partial last cell (the bound then inside a cell: the general path).  A
+    with a partial last cell (the bound then inside a cell: the general path); a float
+    minimum (many offsets are then floats, L = 0, and the rest ties often).  A
     thousand particles at yaw 0 and one x see a point placed to land within a few
     ulps of 0 on x, where only the double add decides the side."""
     rng = np.random.default_rng(sum(dims) + int(tail * 10) + int(abs(mn[0]) > 0))
