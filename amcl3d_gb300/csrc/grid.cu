@@ -124,9 +124,9 @@ int grid_prepare_view(amcl_grid_s* g)
     v.inv_lo[a] = lo;
     v.inv_hi[a] = in.size[a] < (1u << 21) ? hi : INFINITY;
     float lo2 = v.inv_res[a], hi2 = v.inv_res[a];
-    while (static_cast<double>(lo2) > ir * (1.0 - std::ldexp(1.0, -21)))
+    while (static_cast<double>(lo2) > ir * (1.0 - std::ldexp(1.0, -22)))
       lo2 = std::nextafter(lo2, 0.0f);
-    while (static_cast<double>(hi2) < ir * (1.0 + std::ldexp(1.0, -21)))
+    while (static_cast<double>(hi2) < ir * (1.0 + std::ldexp(1.0, -22)))
       hi2 = std::nextafter(hi2, INFINITY);
     v.inv_lo2[a] = lo2;
     v.inv_hi2[a] = hi2;

@@ -66,7 +66,7 @@ struct GridView
   uint32_t pad_cell;  // index of the zero cell stored after the last cell of every prob array
   int fast_idx;       // mag[] exists and pad_cell < 2^32
   // The yaw-only loop for offsets that are not floats (weigh_chunk_yaw2_gen): 1/res
-  // bracketed 2^-21 relative below and above, wide enough for the float estimate of a
+  // bracketed 2^-22 relative below and above, wide enough for the float estimate of a
   // transformed coordinate; usable when every axis's bound V is the threshold of its
   // last cell (V = T[size], so the cell range decides the bounds) and is below 2^21 cells.
   float inv_lo2[3], inv_hi2[3];

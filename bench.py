@@ -621,7 +621,7 @@ def map_minimum_section(ft, seed, zero_min_prof, steps=5, warmup=3, shift=(-17.3
     out = {"minimum": wl[1]["min"], "cloud_weight_ms_per_launch": cw_ms / cw_n,
            "zero_minimum_ms_per_launch": z_ms / z_n, "ratio_to_zero_minimum": (cw_ms / cw_n) / (z_ms / z_n),
            "weights_per_s": r["weights"] / (r["ms"] / 1e3), "steps": steps,
-           "loop": "general yaw loop: float estimate, floors widened 2^-21, float two-sum for open points"}
+           "loop": "general yaw loop: float estimate, floors widened 2^-22, float two-sum for open points"}
     del moved
     torch.cuda.empty_cache()
     return out

@@ -5,7 +5,7 @@ its cell floor(fl64(X / res)) (Grid3d.cpp:181-183).
 
 The loop splits off = double(t) - min as H + L (H = fl32(off), L = fl32(off - H)) and
 takes v = (f + H) + L in float.  Claim 1: wherever |v| >= 2^-20 max|H| and the floors of
-v against 1/res bracketed 2^-21 relative below and above agree, X has v's sign and the
+v against 1/res bracketed 2^-22 relative below and above agree, X has v's sign and the
 floor is the reference's cell.  Claim 2 (the open points): Knuth's two-sum estimate of X
 with its residual test is the reference's X wherever the test does not call the rounding
 undecided.  f runs over uniform coordinates, over the floats around every cell boundary
@@ -21,9 +21,9 @@ def widened(res: float):
     """inv_lo2 / inv_hi2 as the grid's host code builds them."""
     ir = 1.0 / res
     lo = hi = F32(ir)
-    while float(lo) > ir * (1.0 - 2.0**-21):
+    while float(lo) > ir * (1.0 - 2.0**-22):
         lo = np.nextafter(lo, F32(0.0))
-    while float(hi) < ir * (1.0 + 2.0**-21):
+    while float(hi) < ir * (1.0 + 2.0**-22):
         hi = np.nextafter(hi, F32(np.inf))
     return lo, hi
 
@@ -86,7 +86,13 @@ def test_general_yaw_floors_and_open_points(res, mn):
     flo = np.floor(v.astype(np.float64) * float(lo2))  # exact products: 24 x 24 bits
     fhi = np.floor(v.astype(np.float64) * float(hi2))
     zb = F32(2.0**-20) * np.abs(H)
-    settled = (np.abs(v) >= zb) & (flo == fhi)
+    # the estimate's error bound behind the bracket: |v - X| <= 3.125 * 2^-24 |v| + 2^-47 |H|
+    # (below the bracket's 4 * 2^-24) wherever |v| >= 2^-20 |H|
+    far = np.abs(v) >= zb
+    err = np.abs(v[far].astype(np.float64) - X[far].astype(np.float64))
+    bound = 3.125 * 2.0**-24 * np.abs(v[far].astype(np.float64)) + 2.0**-47 * np.abs(H[far].astype(np.float64))
+    assert (err <= bound).all()
+    settled = far & (flo == fhi)
     # claim 1: settled points have X's sign and, inside the map, the reference's cell
     assert np.array_equal(X[settled] < 0, v[settled] < 0)
     inside = settled & (X >= 0)
