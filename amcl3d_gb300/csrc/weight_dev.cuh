@@ -214,7 +214,7 @@ __device__ __forceinline__ void weigh_chunk_yaw2_fast(const float4* s_pts, const
 // map) gives offsets off = double(t) - min that are not floats, and the reference's
 // X = fl32(double(f) + off) is then no single float add.  With off = H + L (H its float
 // rounding, L the float rounding of the rest) the float estimate v = (f + H) + L lies
-// within 3.1 * 2^-24 * |v| + 2^-47 * |H| of X; so wherever |v| >= 2^-20 * |H| the
+// within 3.125 * 2^-24 * |v| + 2^-47 * |H| of X; so wherever |v| >= 2^-20 * |H| the
 // reference's cell lies between the floors of v against 1/res bracketed 2^-22 relative
 // below and above (GridView::inv_lo2 / inv_hi2), X has v's sign, and when the two floors
 // agree they are the cell and the bounds of v are those of X (every axis's bound being
