@@ -78,3 +78,45 @@ def test_round_down_fma_floor_range():
         s = c + q
         assert 2**23 <= s < 2**24
         assert math.floor(s) - c == math.floor(q)
+
+
+def floor_constants(size):
+    """The grid's floor constants m[a] (grid.cu, restated): sum_a (bits(2^23) + m[a]) * stride[a]
+    = 0 mod 2^32 with strides (1, sx, sx * sy), or None where an offset leaves no room for
+    size[a] + 2 floors below 2^24."""
+    sx, sy, sz = size
+    two32, b = 1 << 32, 0x4B000000
+    s1, s2 = sx, sx * sy
+    r = (two32 - (b * ((1 + s1 + s2) % two32)) % two32) % two32
+    m2, r2 = divmod(r, s2)
+    m1, m0 = divmod(r2, s1)
+    m = (m0, m1, m2)
+    if any(mi + n + 2 > (1 << 23) for mi, n in zip(m, size)):
+        return None
+    return m
+
+
+@pytest.mark.parametrize("size", [(2000, 2000, 400), (800, 800, 160), (400, 400, 100), (200, 200, 200),
+                                  (1000, 1000, 200), (44, 40, 16), (120, 100, 60), (522, 384, 153),
+                                  (2097151, 2, 2), (3, 5, 7), (10, 11, 10)])
+def test_floor_bits_are_the_cell_index(size):
+    """The zero-minimum and real-map yaw loops read the cell index off the bit patterns of
+    the three round-down floors fma_rd(X, inv, 2^23 + m[a]) = 2^23 + m[a] + k[a] (floats in
+    [2^23, 2^24) are the integers): weighted by the strides they sum, mod 2^32, to the
+    reference's ix + iy * sx + iz * sx * sy (Grid3d.cpp:187) for every cell, the one-past
+    floors included."""
+    m = floor_constants(size)
+    if size in ((3, 5, 7), (10, 11, 10)):
+        assert m is None  # too small for the constants: the general loop takes such grids
+        return
+    assert m is not None
+    sx, sy, sz = size
+    rng = np.random.default_rng(sum(size))
+    k = np.stack([rng.integers(0, n + 2, 20000) for n in size], 1)
+    k[:3] = [[0, 0, 0], [sx - 1, sy - 1, sz - 1], [sx + 1, sy + 1, sz + 1]]
+    bits = np.stack([(np.float32(2.0**23) + np.float32(m[a]) + k[:, a].astype(np.float32)).view(np.uint32)
+                     for a in range(3)], 1).astype(np.uint64)
+    stride = np.array([1, sx, sx * sy], np.uint64)
+    idx = (bits * stride).sum(1) % (1 << 32)
+    want = (k[:, 0] + k[:, 1] * sx + k[:, 2] * sx * sy).astype(np.uint64) % (1 << 32)
+    np.testing.assert_array_equal(idx, want)
