@@ -9,7 +9,7 @@
 // contributes its oldest one.  Continuous batching: while step k runs on the GPU,
 // requests that arrive are staged for step k + 1, which launches as soon as step k's
 // results have been read back.  A session's requests complete in submission order
-// (one per step).  New sessions go to the lane with the fewest sessions.
+// (one per step).  New sessions go to the lane carrying the fewest particles.
 //
 // Admission: the server's particle budget bounds the capacity of all open sessions
 // together (each lane's arena can hold the whole budget, so a session fits in any
