@@ -111,3 +111,104 @@ def test_general_yaw_floors_and_open_points(res, mn):
     third = n // 3
     assert amb[:third].mean() < 0.05 and amb[uni].mean() < 0.05
     assert not amb[L == 0].any()
+
+
+def floor_threshold(res: float, k: int) -> np.float32:
+    """The smallest float X >= 0 with floor(fl64(X) / res) >= k (the grid's threshold table)."""
+    if k == 0:
+        return F32(0.0)
+    x = F32(k * res)
+    while not np.floor(float(x) / res) >= k:
+        x = np.nextafter(x, F32(np.inf))
+    while True:
+        d = np.nextafter(x, F32(-np.inf))
+        if d >= 0 and np.floor(float(d) / res) >= k:
+            x = d
+        else:
+            return x
+
+
+def general_loop_cells(poses, scan, mn, res, size):
+    """The cell of every (particle, point) pair as the general yaw loop decides it
+    (weigh_chunk_yaw2_gen, open_cell), restated in numpy; -1 where it gathers the pad."""
+    yaw = poses[:, 3].astype(np.float64)
+    cy = np.cos(yaw).astype(F32)[:, None]
+    sy = np.sin(yaw).astype(F32)[:, None]
+    x, y, z = (scan[None, :, a].astype(F32) for a in range(3))
+    s = [(x * cy) + (-(y * sy)), (x * sy) + (y * cy), np.broadcast_to(z, (poses.shape[0], scan.shape[0]))]
+    V = [floor_threshold(res, n) for n in size]
+    k = []
+    near = np.zeros(s[0].shape, bool)
+    valid = np.ones(s[0].shape, bool)
+    X, Hs, vs = [], [], []
+    for a in range(3):
+        off = poses[:, a].astype(np.float64) - mn[a]
+        H, L = split(off)
+        H, L = H[:, None], L[:, None]
+        Hs.append(H)
+        v = (s[a] + H) + L
+        vs.append(v)
+        lo2, hi2 = widened(res)
+        flo = np.floor(v.astype(np.float64) * float(lo2))
+        fhi = np.floor(v.astype(np.float64) * float(hi2))
+        near |= flo != fhi
+        valid &= (v >= 0) & (v < V[a]) & ~np.signbit(v)
+        k.append(flo)
+        Xe, amb = two_sum_x(s[a], np.broadcast_to(H, s[a].shape), np.broadcast_to(L, s[a].shape))
+        Xr = (s[a].astype(np.float64) + off[:, None]).astype(F32)
+        X.append(np.where(amb, Xr, Xe))
+    zb = F32(2.0**-20) * np.maximum(np.maximum(np.abs(Hs[0]), np.abs(Hs[1])), np.abs(Hs[2]))
+    for v in vs:
+        near |= np.abs(v) < zb
+    sx_, sy_ = size[0], size[1]
+    cell = np.where(valid & ~near, k[0] + k[1] * sx_ + k[2] * sx_ * sy_, -1).astype(np.int64)
+    # open points: the reference's cell of the two-sum (or double-add) X
+    ok = np.ones(s[0].shape, bool)
+    kk = []
+    for a in range(3):
+        ok &= (X[a] >= 0) & (X[a] < V[a])
+        kk.append(np.floor(X[a].astype(np.float64) / res))
+    open_cell = np.where(ok, kk[0] + kk[1] * sx_ + kk[2] * sx_ * sy_, -1).astype(np.int64)
+    return np.where(near, open_cell, cell), near
+
+
+@pytest.mark.parametrize("mn", [(-17.35, -9.5, -1.4), (-9.5, -4.25, -1.5), (-0.35, -2.7, -0.15)])
+def test_general_loop_cells_equal_the_reference(mn):
+    """Every (particle, point) cell of the general yaw loop, restated, equals the
+    reference's (the oracle's cells): random poses and points over a 44 x 40 x 16 grid,
+    plus points placed for yaw-0 particles within a few ulps of cell boundaries and of
+    the minimum plane."""
+    import oracle as O
+
+    res = 0.05
+    size = (44, 40, 16)
+    mx = tuple(mn[a] + size[a] * res for a in range(3))
+    assert tuple(int(v) for v in O.grid_sizes(mn, mx, res)) == size
+    rng = np.random.default_rng(int(abs(mn[0]) * 100))
+    P = 400
+    centre = (np.array(mn) + np.array(mx)) / 2
+    poses = np.zeros((P, 4), F32)
+    poses[:, :3] = centre + rng.uniform(-0.3, 0.3, (P, 3))
+    poses[:, 3] = rng.uniform(-3.2, 3.2, P)
+    poses[:64, 3] = 0.0
+    ext = np.array(mx) - np.array(mn)
+    pts = [rng.uniform(-0.6, 0.6, (1500, 3)) * ext / ext.max()]
+    for p in range(64):  # yaw 0: s is the point itself
+        off = poses[p, :3].astype(np.float64) - np.array(mn)
+        q = np.zeros((12, 3))
+        for j in range(12):
+            for a in range(3):
+                kcell = rng.integers(0, size[a] + 1) if j < 9 else 0
+                q[j, a] = F32(kcell * res - off[a])
+        pts.append(q)
+    cloud = np.zeros((sum(c.shape[0] for c in pts), 4), F32)
+    cloud[:, :3] = np.concatenate(pts).astype(F32)
+    nb = cloud.shape[0] - 1500
+    bits = cloud[1500:, :3].view(np.int32) + rng.integers(-3, 4, (nb, 3)).astype(np.int32)
+    cloud[1500:, :3] = bits.view(F32)
+    prob = rng.uniform(0.0, 8.0, int(np.prod(size))).astype(F32)
+    g = O.GridData(mn, mx, res, size, prob, np.zeros_like(prob))
+    _, want = O.cloud_weights(g, poses, cloud, 0.0, 0.0, yaw_trig=1, cells=True)
+    got, near = general_loop_cells(poses, cloud, mn, res, size)
+    np.testing.assert_array_equal(got, want)
+    assert near.sum() > 100  # the placed points reach the open-point path
