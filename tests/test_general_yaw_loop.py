@@ -9,7 +9,9 @@ v against 1/res bracketed 2^-22 relative below and above agree, X has v's sign a
 floor is the reference's cell.  Claim 2 (the open points): Knuth's two-sum estimate of X
 with its residual test is the reference's X wherever the test does not call the rounding
 undecided.  f runs over uniform coordinates, over the floats around every cell boundary
-and around the map's minimum plane (X near 0)."""
+and around the map's minimum plane (X near 0).  Then the loop's whole cell decision
+(floors, bounds, the near-zero bound, open points), restated, against the oracle's cell
+for every particle x point pair."""
 
 import numpy as np
 import pytest
